@@ -1,0 +1,143 @@
+/*
+ * manifoldem_gb300.h -- C ABI of the GB300 (sm_103a) per-projection-direction distance stage.
+ *
+ * One call processes a batch of projection directions (PDs).  For every PD it does what
+ * ManifoldEM's getDistanceCTF_local_Conj9combinedS2.op() does to the PD's particle images
+ * (reference modules/getDistanceCTF_local_Conj9combinedS2.py:216-420):
+ *   read each image from a SPIDER raw float32 stack (transposed, conjugate views flipped
+ *   up-down), normalise it by the mean/std of its background, Butterworth-filter it, mask it,
+ *   rotate it twice (periodic cubic B-spline, angles -deg(Psi_i) then -psi_p), build its CTF,
+ *   and produce:
+ *     D[i][j] = sum_k |CTF_j(k) F_i(k) - CTF_i(k) F_j(k)|^2      (float64, n x n per PD)
+ *     imgAvg   (Wiener average), imgAvgFlip (phase-flipped average), imgAllIntensity
+ *     imgAll, imgAllFlip, CTF per image (float32; the reference stores them as float64).
+ *
+ * Conventions
+ *   - All array arguments are device pointers unless marked HOST.
+ *   - The caller allocates every device buffer, including the workspace; the library keeps only
+ *     host-side state (plans, cached cuFFT plans).  Nothing here calls cudaMalloc.
+ *   - Every function returns MEM_OK (0) or a negative MEM_ERR_* status; nothing throws.
+ *   - Work is enqueued on the caller's stream (a cudaStream_t passed as void*); mem_plan_execute
+ *     issues only kernel launches and cuFFT executions, so it may be captured in a CUDA graph.
+ *   - Host-side geometry (PD, PDs, Psi_i, Nom, Dnom, psi_p, imgLabels) stays with the caller, as in
+ *     the reference, which computes it in numpy/scipy (:297-323, psi_ang :206-213 via
+ *     q2Spider.op's least-squares fit).  The caller passes Psi_i and psi_p in.
+ */
+#ifndef MANIFOLDEM_GB300_H
+#define MANIFOLDEM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MEM_ABI_VERSION 1
+
+/* status codes */
+#define MEM_OK                    0
+#define MEM_ERR_INVALID          -1  /* bad argument (null pointer, size out of range)          */
+#define MEM_ERR_UNSUPPORTED      -2  /* box size or option this build does not support           */
+#define MEM_ERR_WORKSPACE        -3  /* workspace smaller than mem_plan_workspace_size()        */
+#define MEM_ERR_CUDA             -4  /* a CUDA runtime call failed                               */
+#define MEM_ERR_CUFFT            -5  /* a cuFFT call failed                                      */
+#define MEM_ERR_DEVICE_TIMEOUT   -6  /* a bounded device-side wait expired (kernel returned)     */
+#define MEM_ERR_NO_DEVICE        -7  /* no sm_103 device is current                              */
+
+/* contraction forms for D */
+#define MEM_PREC_FP32        0   /* plain FP32 SIMT contraction, FP64 epilogue                   */
+#define MEM_PREC_SPLIT_BF16  1   /* 3-term split-BF16 on tcgen05 tensor cores, FP64 epilogue     */
+
+/* low-pass filter types, filterPar['type'] (reference :156-167) */
+#define MEM_FILTER_BUTTER 0
+#define MEM_FILTER_GAUSS  1
+
+/* Microscope and stage parameters: the reference's module globals p.nPix, p.pix_size, p.Cs,
+ * p.EkV, p.gaussEnv, p.AmpContrast, plus filterPar and options['avgOnly'].               */
+typedef struct mem_params {
+    int32_t N;              /* box size (p.nPix), 8 <= N <= 236                              */
+    int32_t filter_type;    /* MEM_FILTER_*                                                  */
+    double  filter_Qc;      /* cutoff in units of Nyquist (filterPar['Qc'])                   */
+    double  filter_order;   /* Butterworth order (filterPar['N'])                             */
+    double  pix_size;       /* Angstrom per pixel                                              */
+    double  Cs;             /* spherical aberration, mm                                        */
+    double  EkV;            /* acceleration voltage, kV                                        */
+    double  gaussEnv;       /* Gaussian envelope half-width, 1/A; +inf disables the envelope   */
+    double  AmpContrast;    /* amplitude contrast ratio                                        */
+    int32_t avg_only;       /* options['avgOnly']: skip D                                      */
+    int32_t precision;      /* MEM_PREC_*                                                      */
+} mem_params;
+
+/* Per-call device inputs.  Images of PD p are the pd_count[p] consecutive entries starting at
+ * the sum of the previous counts, in the order of the PD's index list ``ind``.           */
+typedef struct mem_inputs {
+    const float*   stack;        /* SPIDER raw stack, num_stack * N * N float32              */
+    int64_t        num_stack;
+    const int64_t* stack_index;  /* [n_images] stack image of each entry: ind, or
+                                    ind - nStot/2 for conjugate views (reference :247-252)      */
+    const uint8_t* flip;         /* [n_images] 1 for conjugate views (ind >= nStot/2)         */
+    const double*  psi_rad;      /* [n_images] Psi_i = 2 atan(s/c), NaN replaced by 0 (:317-321) */
+    const double*  df;           /* [n_images] defocus, Angstrom                               */
+} mem_inputs;
+
+/* Per-call device outputs; any pointer may be NULL to skip that output.                   */
+typedef struct mem_outputs {
+    double* D;                 /* PD p at offset sum_{q<p} n_q^2, row-major n_p x n_p         */
+    double* img_avg;           /* [n_pd][N][N]  imgAvg                                         */
+    double* img_avg_flip;      /* [n_pd][N][N]  imgAvgFlip                                     */
+    double* img_all_intensity; /* [n_pd][N][N]  imgAllIntensity                                */
+    float*  img_all;           /* [n_images][N][N] imgAll                                      */
+    float*  img_all_flip;      /* [n_images][N][N] imgAllFlip                                  */
+    float*  ctf;               /* [n_images][N][N] CTF, full plane, FFT (ifftshifted) order    */
+    float*  spectrum;          /* [n_images][N][N/2+1] complex (re,im) half-plane fft2(imgAll)  */
+    double* pair_norm;         /* [n_images] per-image FP64 term a_i of D_ij = a_i + a_j + E_ij */
+} mem_outputs;
+
+typedef struct mem_plan mem_plan;   /* opaque */
+
+/* ---- library ------------------------------------------------------------------------- */
+int         mem_abi_version(void);
+const char* mem_status_string(int status);
+
+/* ---- plans ----------------------------------------------------------------------------
+ * mem_plan_create replaces the per-PD job set-up of GetDistancesS2.op / divide()
+ * (modules/GetDistancesS2.py:37-47, :94) for a batch of PDs: it fixes the box size, the PD
+ * sizes and psi_p of every PD (HOST arrays), lays out the workspace and builds the tile
+ * schedule of the D contraction.                                                          */
+int mem_plan_create(const mem_params* params, int32_t n_pd,
+                    const int32_t* pd_count /* HOST [n_pd] */,
+                    const double* psi_p_deg /* HOST [n_pd], psi_ang(PD) in degrees */,
+                    mem_plan** out_plan);
+int mem_plan_destroy(mem_plan* plan);
+int mem_plan_workspace_size(const mem_plan* plan, size_t* bytes);
+int64_t mem_plan_num_images(const mem_plan* plan);
+int64_t mem_plan_d_elements(const mem_plan* plan);   /* sum n_p^2 */
+int64_t mem_plan_num_pairs(const mem_plan* plan);    /* sum n_p (n_p - 1) / 2 */
+
+/* Copy the plan's tables into the workspace (stream-ordered).  Call once per workspace
+ * before mem_plan_execute (and before capturing it).                                      */
+int mem_plan_upload(mem_plan* plan, void* workspace, size_t workspace_bytes, void* stream);
+
+/* The distance stage for every PD of the plan: replaces
+ * getDistanceCTF_local_Conj9combinedS2.op (modules/getDistanceCTF_local_Conj9combinedS2.py:216)
+ * for the PDs of the plan, minus its pickle write (myio.fout1, :409-412), which stays with the
+ * caller.  Stream-ordered and graph-capturable.                                            */
+int mem_plan_execute(mem_plan* plan, const mem_inputs* in, const mem_outputs* out,
+                     void* workspace, size_t workspace_bytes, void* stream);
+
+/* Reads the device status word of the workspace (after the stream has been synchronised):
+ * MEM_OK, or MEM_ERR_DEVICE_TIMEOUT if a bounded device-side wait gave up.                 */
+int mem_workspace_status(const mem_plan* plan, const void* workspace);
+
+/* One-shot convenience: plan, upload and execute on `stream`, then destroy the plan.
+ * The workspace must be at least the size mem_plan_workspace_size reports for the same
+ * arguments.                                                                               */
+int mem_pd_batch(const mem_params* params, int32_t n_pd, const int32_t* pd_count,
+                 const double* psi_p_deg, const mem_inputs* in, const mem_outputs* out,
+                 void* workspace, size_t workspace_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MANIFOLDEM_GB300_H */

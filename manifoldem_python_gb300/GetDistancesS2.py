@@ -1,0 +1,117 @@
+"""Driver of the distance stage over all projection directions, on one GPU.
+
+Mirrors ``GetDistancesS2.op`` (reference ``modules/GetDistancesS2.py:53-124``): it loads the
+tessellation file (``CG``, ``q``, ``df``, ``sh``), builds the job list of the PDs that have no
+resume marker (``fileCheck``/``divide``, ``:29-47``), runs them, writes one pickle per PD plus its
+marker and reports progress through an optional Qt-style signal (``argv[0].emit(percent)``).
+
+Instead of a process pool it submits the pending PDs to the GPU in HBM-admitted batches; each
+batch is one plan/execute of the C ABI.  The resume semantics are the reference's: a PD counts
+as done when ``<dist_prog>/<prD>`` exists, and markers are written after the pickle.
+"""
+from __future__ import annotations
+
+import os
+import time
+from typing import List, Optional
+
+import numpy as np
+
+from . import myio, set_params
+from .getDistanceCTF_local_Conj9combinedS2 import (OUTPUT_KEYS, assemble, read_spider_images,
+                                                    stage_params)
+from .p import params_module
+from .pipeline import DEFAULT_OUTPUTS, DistanceStage, PdJob, admit_batches
+
+FILTER_PAR = dict(type='Butter', Qc=0.5, N=8)
+
+
+def fileCheck() -> List[int]:
+    p = params_module()
+    fin = []
+    for root, dirs, files in os.walk(p.dist_prog):
+        for f in sorted(files):
+            if not f.startswith('.'):
+                fin.append(int(f))
+    return fin
+
+
+def divide(CG, q, df, N) -> list:
+    p = params_module()
+    ll = []
+    fin = fileCheck()
+    for prD in range(N):
+        ind = CG[prD]
+        dist_file = '{}prD_{}'.format(p.dist_file, prD)
+        if prD not in fin:
+            ll.append([ind, q[:, ind], df[ind], dist_file, prD])
+    return ll
+
+
+def count(N) -> int:
+    return N - len(fileCheck())
+
+
+def run_jobs(jobs: list, stack_file: str, nStot: int, options: dict, progress=None,
+             budget_bytes: Optional[int] = None, precision: Optional[str] = None,
+             done_offset: int = 0, total: Optional[int] = None) -> None:
+    """Run ``jobs`` ([ind, q, df, outFile, prD] each) in HBM-admitted GPU batches."""
+    import torch
+
+    p = params_module()
+    N = int(p.nPix)
+    params = stage_params(p, FILTER_PAR, options, precision)
+    stage = DistanceStage(params)
+    if budget_bytes is None:
+        free, _ = torch.cuda.mem_get_info(stage.device)
+        budget_bytes = int(free * 0.6)
+    counts = [int(np.asarray(j[0]).shape[0]) for j in jobs]
+    done = done_offset
+    total = total or len(jobs)
+    for batch in admit_batches(counts, params, budget_bytes):
+        pj = [PdJob(ind=np.asarray(jobs[i][0]), q=np.asarray(jobs[i][1], dtype=np.float64),
+                    df=np.asarray(jobs[i][2], dtype=np.float64), outFile=jobs[i][3],
+                    prD=jobs[i][4]) for i in batch]
+        geoms = stage.geometry(pj, nStot)
+        all_idx = np.concatenate([g.stack_index for g in geoms])
+        imgs, compact = read_spider_images(stack_file, all_idx, N)
+        off = 0
+        for g in geoms:
+            g.stack_index = compact[off:off + g.stack_index.size]
+            off += g.stack_index.size
+        stack = torch.from_numpy(imgs).to(stage.device)
+        results = stage.run(pj, stack, nStot, outputs=DEFAULT_OUTPUTS, geoms=geoms)
+        for job, geom, res in zip(pj, geoms, results):
+            out = assemble(job, geom, res, N, options)
+            myio.fout1(job.outFile, OUTPUT_KEYS, [out[k] for k in OUTPUT_KEYS])
+            open(os.path.join(p.dist_prog, '%s' % job.prD), 'a').close()
+            done += 1
+            if progress is not None:
+                progress.emit(int((done / float(total)) * 100))
+        del stack, results
+
+
+def op(*argv):
+    p = params_module()
+    set_params.op(1)
+    data = myio.fin1(p.tess_file)
+    CG = data['CG']
+    df = data['df']
+    q = data['q']
+    size = len(df)
+    options = dict(verbose=False, avgOnly=False, visual=False, parallel=False,
+                   relion_data=p.relion_data, thres=p.PDsizeThH)
+    if p.relion_data is False:
+        p.nPix = int(np.sqrt(os.path.getsize(p.img_stack_file) / (4 * p.num_part)))
+        set_params.op(0)
+    input_data = divide(CG, q, df, p.numberofJobs)
+    progress = argv[0] if argv else None
+    offset = p.numberofJobs - len(input_data)
+    if progress is not None:
+        progress.emit(int((offset / float(max(p.numberofJobs, 1))) * 100))
+    print("Processing {} projection directions.".format(len(input_data)))
+    if input_data:
+        run_jobs(input_data, p.img_stack_file, size, options, progress=progress,
+                 done_offset=offset, total=p.numberofJobs)
+    set_params.op(0)
+    return

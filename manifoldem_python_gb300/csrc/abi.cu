@@ -1,0 +1,444 @@
+// C ABI of the distance stage: plans, workspace layout, cuFFT plan cache and the per-call
+// pipeline.  See include/manifoldem_gb300.h for the contract.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <new>
+#include <tuple>
+
+#include "mem_internal.cuh"
+
+namespace mem {
+namespace {
+
+constexpr size_t kAlign = 256;
+inline size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
+
+// ---- cuFFT plan cache: (N, kind, batch) -> plan, work size ----------------------------
+struct FftPlan {
+    cufftHandle h = 0;
+    size_t work = 0;
+};
+std::mutex g_fft_mu;
+std::map<std::tuple<int, int, int, int>, FftPlan> g_fft;   // (device, N, kind, batch)
+
+int fft_plan(int device, int N, cufftType type, int batch, FftPlan* out) {
+    std::lock_guard<std::mutex> lk(g_fft_mu);
+    auto key = std::make_tuple(device, N, (int)type, batch);
+    auto it = g_fft.find(key);
+    if (it != g_fft.end()) {
+        *out = it->second;
+        return MEM_OK;
+    }
+    FftPlan p;
+    if (cufftCreate(&p.h) != CUFFT_SUCCESS) return MEM_ERR_CUFFT;
+    if (cufftSetAutoAllocation(p.h, 0) != CUFFT_SUCCESS) return MEM_ERR_CUFFT;
+    int n[2] = {N, N};
+    const int Nh = N / 2 + 1;
+    cufftResult r;
+    if (type == CUFFT_R2C)
+        r = cufftMakePlanMany(p.h, 2, n, nullptr, 1, N * N, nullptr, 1, N * Nh, type, batch,
+                              &p.work);
+    else
+        r = cufftMakePlanMany(p.h, 2, n, nullptr, 1, N * Nh, nullptr, 1, N * N, type, batch,
+                              &p.work);
+    if (r != CUFFT_SUCCESS) {
+        cufftDestroy(p.h);
+        return MEM_ERR_CUFFT;
+    }
+    g_fft[key] = p;
+    *out = p;
+    return MEM_OK;
+}
+
+size_t fft_work_estimate(int N, cufftType type, int batch) {
+    int n[2] = {N, N};
+    const int Nh = N / 2 + 1;
+    size_t ws = 0;
+    cufftResult r = type == CUFFT_R2C
+        ? cufftEstimateMany(2, n, nullptr, 1, N * N, nullptr, 1, N * Nh, type, batch, &ws)
+        : cufftEstimateMany(2, n, nullptr, 1, N * Nh, nullptr, 1, N * N, type, batch, &ws);
+    return r == CUFFT_SUCCESS ? ws : 0;
+}
+
+// batch sizes exec_fft uses for `count` transforms: full chunks and the remainder
+void fft_batches(int64_t count, std::vector<int>* batches) {
+    if (count >= kFftChunk) batches->push_back(kFftChunk);
+    if (count % kFftChunk) batches->push_back((int)(count % kFftChunk));
+}
+
+int exec_fft(const mem_plan& P, cufftType type, int64_t count, int64_t in_stride,
+             int64_t out_stride, void* in, void* out, void* work, cudaStream_t s) {
+    for (int64_t b = 0; b < count; b += kFftChunk) {
+        const int batch = (int)std::min<int64_t>(kFftChunk, count - b);
+        FftPlan fp;
+        int st = fft_plan(P.device, P.N, type, batch, &fp);
+        if (st != MEM_OK) return st;
+        if (cufftSetStream(fp.h, s) != CUFFT_SUCCESS) return MEM_ERR_CUFFT;
+        if (cufftSetWorkArea(fp.h, work) != CUFFT_SUCCESS) return MEM_ERR_CUFFT;
+        cufftResult r;
+        if (type == CUFFT_R2C)
+            r = cufftExecR2C(fp.h, (cufftReal*)in + b * in_stride,
+                             (cufftComplex*)out + b * out_stride);
+        else
+            r = cufftExecC2R(fp.h, (cufftComplex*)in + b * in_stride,
+                             (cufftReal*)out + b * out_stride);
+        if (r != CUFFT_SUCCESS) return MEM_ERR_CUFFT;
+    }
+    return MEM_OK;
+}
+
+template <class T>
+T* at(void* ws, size_t off) {
+    return reinterpret_cast<T*>(static_cast<char*>(ws) + off);
+}
+
+CtfConst make_ctf(const mem_params& p, int N) {
+    CtfConst c{};
+    const double lam = 12.3986 / std::sqrt((2 * 511.0 + p.EkV) * p.EkV);
+    const double Npix = (double)N * p.pix_size;
+    const double P = p.Cs * 1.0e7 * lam * lam * lam / (4.0 * Npix * Npix * Npix * Npix);
+    const double d = std::atan(p.AmpContrast) / (2.0 * M_PI);
+    auto fix = [](double x) -> uint64_t {
+        double fr = x - std::floor(x);
+        double v = std::ldexp(fr, 64);
+        if (v >= 18446744073709551615.0) return 0ull;
+        return (uint64_t)v;
+    };
+    c.p_fix = fix(P);
+    c.d_fix = fix(d);
+    c.q_scale = lam / (2.0 * Npix * Npix);
+    c.amp = (float)std::sqrt(1.0 + p.AmpContrast * p.AmpContrast);
+    if (std::isinf(p.gaussEnv) || p.gaussEnv <= 0.0) {
+        c.env_c = 0.0f;
+    } else {
+        const double sigm = p.gaussEnv / std::sqrt(2.0 * std::log(2.0));
+        c.env_c = (float)(1.0 / (Npix * Npix * 2.0 * sigm * sigm));
+    }
+    return c;
+}
+
+int check_device(int* device, int* sms) {
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return MEM_ERR_NO_DEVICE;
+    }
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess) return MEM_ERR_CUDA;
+    *device = dev;
+    *sms = prop.multiProcessorCount;
+    return MEM_OK;
+}
+
+}  // namespace
+}  // namespace mem
+
+using namespace mem;
+
+extern "C" {
+
+int mem_abi_version(void) { return MEM_ABI_VERSION; }
+
+const char* mem_status_string(int status) {
+    switch (status) {
+        case MEM_OK: return "ok";
+        case MEM_ERR_INVALID: return "invalid argument";
+        case MEM_ERR_UNSUPPORTED: return "unsupported box size or option";
+        case MEM_ERR_WORKSPACE: return "workspace too small";
+        case MEM_ERR_CUDA: return "CUDA runtime error";
+        case MEM_ERR_CUFFT: return "cuFFT error";
+        case MEM_ERR_DEVICE_TIMEOUT: return "bounded device-side wait expired";
+        case MEM_ERR_NO_DEVICE: return "no CUDA device";
+        default: return "unknown status";
+    }
+}
+
+int mem_plan_create(const mem_params* params, int32_t n_pd, const int32_t* pd_count,
+                    const double* psi_p_deg, mem_plan** out_plan) {
+    if (!params || !pd_count || !psi_p_deg || !out_plan || n_pd < 1) return MEM_ERR_INVALID;
+    *out_plan = nullptr;
+    const mem_params& p = *params;
+    if (p.N < 8) return MEM_ERR_INVALID;
+    if (p.N > kMaxN) return MEM_ERR_UNSUPPORTED;
+    if (p.filter_type != MEM_FILTER_BUTTER && p.filter_type != MEM_FILTER_GAUSS)
+        return MEM_ERR_INVALID;
+    if (p.precision != MEM_PREC_FP32 && p.precision != MEM_PREC_SPLIT_BF16)
+        return MEM_ERR_INVALID;
+    if (!(p.pix_size > 0) || !(p.EkV > 0) || !(p.filter_Qc > 0)) return MEM_ERR_INVALID;
+    for (int i = 0; i < n_pd; ++i) {
+        if (pd_count[i] < 1) return MEM_ERR_INVALID;
+        if (!std::isfinite(psi_p_deg[i])) return MEM_ERR_INVALID;
+    }
+    mem_plan* P = new (std::nothrow) mem_plan();
+    if (!P) return MEM_ERR_INVALID;
+    P->params = p;
+    P->n_pd = n_pd;
+    P->N = p.N;
+    P->Nh = p.N / 2 + 1;
+    P->Kc = (int64_t)P->N * P->Nh;
+    P->Kc_pad = (P->Kc + kKPad - 1) / kKPad * kKPad;
+    P->count.assign(pd_count, pd_count + n_pd);
+    P->pd.resize(n_pd);
+    int64_t img = 0, row = 0, d = 0, pairs = 0;
+    for (int i = 0; i < n_pd; ++i) {
+        const int n = pd_count[i];
+        PdDev& q = P->pd[i];
+        q.img_off = img;
+        q.row_off = row;
+        q.d_off = d;
+        q.n = n;
+        q.pad = 0;
+        const double t = (-psi_p_deg[i]) * (M_PI / 180.0);
+        q.rot2_cos = std::cos(t);
+        q.rot2_sin = std::sin(t);
+        const int nb = (n + kRowBlock - 1) / kRowBlock;
+        for (int I = 0; I < nb; ++I)
+            for (int J = I; J < nb; ++J) P->tiles.push_back(Tile{i, I, J, 0});
+        for (int64_t b = 0; b < n; b += kSumChunk)
+            P->items.push_back(SumItem{i, 0, img + b, img + std::min<int64_t>(n, b + kSumChunk)});
+        for (int k = 0; k < n; ++k) {
+            P->img_pd.push_back(i);
+            P->img_row.push_back((int32_t)(row + k));
+        }
+        img += n;
+        row += (int64_t)nb * kRowBlock;
+        d += (int64_t)n * n;
+        pairs += (int64_t)n * (n - 1) / 2;
+    }
+    P->n_images = img;
+    P->n_rows = row;
+    P->d_elems = d;
+    P->n_pairs = pairs;
+    if (row > INT32_MAX) {
+        delete P;
+        return MEM_ERR_UNSUPPORTED;
+    }
+    P->ctf = make_ctf(p, P->N);
+
+    // cuFFT work sizes: exact when a device is current, an estimate otherwise
+    std::vector<int> img_batches;
+    fft_batches(P->n_images, &img_batches);
+    fft_batches(2 * (int64_t)n_pd, &img_batches);
+    const bool have_dev = check_device(&P->device, &P->num_sms) == MEM_OK;
+    if (!have_dev) {
+        P->device = -1;
+        P->num_sms = 152;
+    }
+    size_t work = 0;
+    for (int b : img_batches) {
+        for (cufftType ty : {CUFFT_R2C, CUFFT_C2R}) {
+            if (have_dev) {
+                FftPlan fp;
+                const int st = fft_plan(P->device, P->N, ty, b, &fp);
+                if (st != MEM_OK) {
+                    delete P;
+                    return st;
+                }
+                work = std::max(work, fp.work);
+            } else {
+                work = std::max(work, 2 * fft_work_estimate(P->N, ty, b));
+            }
+        }
+    }
+    P->cufft_work_bytes = work;
+
+    // workspace layout
+    Layout& L = P->lay;
+    const int64_t NN = (int64_t)P->N * P->N;
+    const size_t feat_elem = (p.precision == MEM_PREC_FP32) ? 4 : 2;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        const size_t o = off;
+        off = align_up(off + std::max<size_t>(bytes, 1));
+        return o;
+    };
+    L.status = take(sizeof(uint32_t) * 4);
+    L.pd_table = take(sizeof(PdDev) * n_pd);
+    L.sum_items = take(sizeof(SumItem) * P->items.size());
+    L.item_off = take(sizeof(int32_t) * (n_pd + 1));
+    L.img_pd = take(sizeof(int32_t) * P->n_images);
+    L.img_row = take(sizeof(int32_t) * P->n_images);
+    L.tiles = take(sizeof(Tile) * P->tiles.size());
+    L.qfix = take(sizeof(uint64_t) * P->n_images);
+    L.gtab = take(sizeof(float) * P->N * P->Nh);
+    L.pd_max = take(sizeof(uint32_t) * n_pd);
+    L.xbuf = take(sizeof(float) * NN * P->n_images);
+    L.spec = take(sizeof(float) * 2 * P->Kc * P->n_images);
+    L.feat_a = take(feat_elem * 4 * P->Kc_pad * P->n_rows);
+    L.feat_b = (p.precision == MEM_PREC_FP32) ? L.feat_a : take(feat_elem * 4 * P->Kc_pad * P->n_rows);
+    L.pair_norm = take(sizeof(double) * P->n_images);
+    L.partial = take(sizeof(float) * 6 * P->Kc * P->items.size());
+    L.means = take(sizeof(float) * means_stride(*P) * n_pd);
+    L.avg_spec = take(sizeof(float) * 2 * 2 * P->Kc * n_pd);
+    L.avg_real = take(sizeof(float) * 2 * NN * n_pd);
+    L.cufft_work = take(P->cufft_work_bytes);
+    L.total = off;
+    *out_plan = P;
+    return MEM_OK;
+}
+
+int mem_plan_destroy(mem_plan* plan) {
+    delete plan;
+    return MEM_OK;
+}
+
+int mem_plan_workspace_size(const mem_plan* plan, size_t* bytes) {
+    if (!plan || !bytes) return MEM_ERR_INVALID;
+    *bytes = plan->lay.total;
+    return MEM_OK;
+}
+
+int64_t mem_plan_num_images(const mem_plan* plan) { return plan ? plan->n_images : -1; }
+int64_t mem_plan_d_elements(const mem_plan* plan) { return plan ? plan->d_elems : -1; }
+int64_t mem_plan_num_pairs(const mem_plan* plan) { return plan ? plan->n_pairs : -1; }
+
+int mem_plan_upload(mem_plan* plan, void* workspace, size_t workspace_bytes, void* stream) {
+    if (!plan || !workspace) return MEM_ERR_INVALID;
+    if (workspace_bytes < plan->lay.total) return MEM_ERR_WORKSPACE;
+    if (plan->device < 0) {
+        int st = check_device(&plan->device, &plan->num_sms);
+        if (st != MEM_OK) return st;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    const mem_plan& P = *plan;
+    const Layout& L = P.lay;
+    std::vector<int32_t> item_off(P.n_pd + 1, 0);
+    for (const SumItem& it : P.items) item_off[it.pd + 1]++;
+    for (int i = 0; i < P.n_pd; ++i) item_off[i + 1] += item_off[i];
+    MEM_CUDA_TRY(cudaMemcpyAsync(at<char>(workspace, L.pd_table), P.pd.data(),
+                                 sizeof(PdDev) * P.n_pd, cudaMemcpyHostToDevice, s));
+    MEM_CUDA_TRY(cudaMemcpyAsync(at<char>(workspace, L.sum_items), P.items.data(),
+                                 sizeof(SumItem) * P.items.size(), cudaMemcpyHostToDevice, s));
+    MEM_CUDA_TRY(cudaMemcpyAsync(at<char>(workspace, L.item_off), item_off.data(),
+                                 sizeof(int32_t) * item_off.size(), cudaMemcpyHostToDevice, s));
+    MEM_CUDA_TRY(cudaMemcpyAsync(at<char>(workspace, L.img_pd), P.img_pd.data(),
+                                 sizeof(int32_t) * P.n_images, cudaMemcpyHostToDevice, s));
+    MEM_CUDA_TRY(cudaMemcpyAsync(at<char>(workspace, L.img_row), P.img_row.data(),
+                                 sizeof(int32_t) * P.n_images, cudaMemcpyHostToDevice, s));
+    MEM_CUDA_TRY(cudaMemcpyAsync(at<char>(workspace, L.tiles), P.tiles.data(),
+                                 sizeof(Tile) * P.tiles.size(), cudaMemcpyHostToDevice, s));
+    // padding rows of the feature matrices stay zero for the whole life of the workspace
+    const size_t feat_elem = (P.params.precision == MEM_PREC_FP32) ? 4 : 2;
+    const size_t row_bytes = feat_elem * 4 * P.Kc_pad;
+    for (int i = 0; i < P.n_pd; ++i) {
+        const int n = P.pd[i].n;
+        const int64_t padded = (int64_t)((n + kRowBlock - 1) / kRowBlock) * kRowBlock;
+        if (padded == n) continue;
+        const size_t o = (size_t)(P.pd[i].row_off + n) * row_bytes;
+        const size_t len = (size_t)(padded - n) * row_bytes;
+        MEM_CUDA_TRY(cudaMemsetAsync(at<char>(workspace, L.feat_a) + o, 0, len, s));
+        if (L.feat_b != L.feat_a)
+            MEM_CUDA_TRY(cudaMemsetAsync(at<char>(workspace, L.feat_b) + o, 0, len, s));
+    }
+    // the pageable sources above are consumed before cudaMemcpyAsync returns
+    return MEM_OK;
+}
+
+int mem_plan_execute(mem_plan* plan, const mem_inputs* in, const mem_outputs* out,
+                     void* workspace, size_t workspace_bytes, void* stream) {
+    if (!plan || !in || !out || !workspace) return MEM_ERR_INVALID;
+    if (workspace_bytes < plan->lay.total) return MEM_ERR_WORKSPACE;
+    if (!in->stack || !in->stack_index || !in->flip || !in->psi_rad || !in->df)
+        return MEM_ERR_INVALID;
+    if (in->num_stack < 1) return MEM_ERR_INVALID;
+    if (plan->device < 0) return MEM_ERR_INVALID;   // not uploaded
+    const mem_plan& P = *plan;
+    const Layout& L = P.lay;
+    cudaStream_t s = (cudaStream_t)stream;
+    void* ws = workspace;
+    uint32_t* status = at<uint32_t>(ws, L.status);
+    const PdDev* pds = at<PdDev>(ws, L.pd_table);
+    const int32_t* img_pd = at<int32_t>(ws, L.img_pd);
+    const int32_t* img_row = at<int32_t>(ws, L.img_row);
+    float* xbuf = at<float>(ws, L.xbuf);
+    float2* spec = at<float2>(ws, L.spec);
+    uint64_t* qf = at<uint64_t>(ws, L.qfix);
+    void* work = at<char>(ws, L.cufft_work);
+    const int64_t NN = (int64_t)P.N * P.N;
+    const int64_t specN = P.Kc;
+    int st;
+#define MEM_STEP(x)                 \
+    do {                            \
+        st = (x);                   \
+        if (st != MEM_OK) return st; \
+    } while (0)
+
+    MEM_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(uint32_t) * 4, s));
+    // (a2) gather, conjugate flip, normalisation
+    MEM_STEP(kern::gather_normalize(P, *in, xbuf, status, s));
+    // (a3) low-pass filter: R2C, multiply by G/N^2, C2R
+    MEM_STEP(exec_fft(P, CUFFT_R2C, P.n_images, NN, specN, xbuf, spec, work, s));
+    MEM_STEP(kern::lowpass(P, spec, at<float>(ws, L.gtab), s));
+    MEM_STEP(exec_fft(P, CUFFT_C2R, P.n_images, specN, NN, spec, xbuf, work, s));
+    // (a4, a6) mask and the two rotations -> imgAll
+    float* img_all = out->img_all ? out->img_all : xbuf;
+    MEM_STEP(kern::rotate(P, *in, xbuf, img_all, pds, img_pd, s));
+    // (a8) F = fft2(imgAll)
+    MEM_STEP(exec_fft(P, CUFFT_R2C, P.n_images, NN, specN, img_all, spec, work, s));
+    // (a7, a9) CTF, per-PD sums, centring vectors, average spectra
+    MEM_STEP(kern::qfix(P, *in, qf, s));
+    float* partial = at<float>(ws, L.partial);
+    MEM_STEP(kern::pd_sums(P, spec, qf, at<SumItem>(ws, L.sum_items), partial, s));
+    float* means = at<float>(ws, L.means);
+    float2* avg_spec = at<float2>(ws, L.avg_spec);
+    uint32_t* pd_max = at<uint32_t>(ws, L.pd_max);
+    MEM_STEP(kern::pd_finalize(P, partial, at<SumItem>(ws, L.sum_items),
+                               at<int32_t>(ws, L.item_off), pds, means, avg_spec, pd_max, s));
+    // features of D, a_i, sign(C) F, CTF output
+    void* feat_a = at<char>(ws, L.feat_a);
+    void* feat_b = at<char>(ws, L.feat_b);
+    double* pair_norm = out->pair_norm ? out->pair_norm : at<double>(ws, L.pair_norm);
+    MEM_STEP(kern::features(P, spec, qf, pds, img_pd, img_row, means, pd_max, feat_a, feat_b,
+                            pair_norm, out->ctf, out->spectrum, s));
+    // averages: one inverse transform per PD (linearity of the reference's per-image sums)
+    float* avg_real = at<float>(ws, L.avg_real);
+    if (out->img_avg || out->img_avg_flip) {
+        MEM_STEP(exec_fft(P, CUFFT_C2R, 2 * P.n_pd, specN, NN, avg_spec, avg_real, work, s));
+        MEM_STEP(kern::avg_store(P, avg_real, out->img_avg, out->img_avg_flip, s));
+    }
+    // phase-flipped images and their mean intensity
+    if (out->img_all_flip || out->img_all_intensity) {
+        float* flip_imgs = out->img_all_flip ? out->img_all_flip : xbuf;
+        MEM_STEP(exec_fft(P, CUFFT_C2R, P.n_images, specN, NN, spec, flip_imgs, work, s));
+        MEM_STEP(kern::intensity(P, flip_imgs, pds, out->img_all_intensity, s));
+    }
+    // (a10) D
+    if (!P.params.avg_only && out->D) {
+        const Tile* tiles = at<Tile>(ws, L.tiles);
+        if (P.params.precision == MEM_PREC_FP32)
+            MEM_STEP(kern::gemm_fp32(P, (const float*)feat_a, pair_norm, pd_max, tiles, pds,
+                                     out->D, s));
+        else
+            MEM_STEP(kern::gemm_split_bf16(P, feat_a, feat_b, pair_norm, pd_max, tiles, pds,
+                                           out->D, status, s));
+    }
+#undef MEM_STEP
+    return MEM_OK;
+}
+
+int mem_workspace_status(const mem_plan* plan, const void* workspace) {
+    if (!plan || !workspace) return MEM_ERR_INVALID;
+    uint32_t st = 0;
+    MEM_CUDA_TRY(cudaMemcpy(&st, static_cast<const char*>(workspace) + plan->lay.status,
+                            sizeof(st), cudaMemcpyDeviceToHost));
+    if (st & kStatusTimeout) return MEM_ERR_DEVICE_TIMEOUT;
+    if (st & 2u) return MEM_ERR_INVALID;
+    return MEM_OK;
+}
+
+int mem_pd_batch(const mem_params* params, int32_t n_pd, const int32_t* pd_count,
+                 const double* psi_p_deg, const mem_inputs* in, const mem_outputs* out,
+                 void* workspace, size_t workspace_bytes, void* stream) {
+    mem_plan* plan = nullptr;
+    int st = mem_plan_create(params, n_pd, pd_count, psi_p_deg, &plan);
+    if (st != MEM_OK) return st;
+    st = mem_plan_upload(plan, workspace, workspace_bytes, stream);
+    if (st == MEM_OK) st = mem_plan_execute(plan, in, out, workspace, workspace_bytes, stream);
+    mem_plan_destroy(plan);
+    return st;
+}
+
+}  // extern "C"

@@ -1,0 +1,140 @@
+// Internal declarations shared by the distance-stage translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cufft.h>
+#include <cstdint>
+#include <vector>
+
+#include "../../include/manifoldem_gb300.h"
+
+namespace mem {
+
+constexpr int kMaxN = 236;          // rotation kernel keeps one N x (N|1) float image in smem
+constexpr int kRowBlock = 128;      // PD rows are padded to this in the feature matrix
+constexpr int kKPad = 64;           // each feature block is padded to a multiple of this
+constexpr int kSumChunk = 256;      // images per partial-sum item of the per-PD reductions
+constexpr int kFftChunk = 8192;     // images per batched cuFFT execution
+
+// device status word bits (first 4 bytes of the workspace)
+constexpr uint32_t kStatusTimeout = 1u;
+
+// ---- per-PD table uploaded to the workspace --------------------------------------------
+struct PdDev {
+    int64_t img_off;     // first image of the PD
+    int64_t row_off;     // first feature-matrix row of the PD (multiple of kRowBlock)
+    int64_t d_off;       // first element of the PD's D block
+    int32_t n;           // images in the PD
+    int32_t pad;
+    double  rot2_cos, rot2_sin;   // rotation by -psi_p
+};
+
+// partial-sum item: images [img_begin, img_end) of PD pd
+struct SumItem {
+    int32_t pd;
+    int32_t pad;
+    int64_t img_begin, img_end;
+};
+
+// D contraction tile: PD pd, row block I, column block J (I <= J)
+struct Tile {
+    int32_t pd, I, J, pad;
+};
+
+// CTF constants (phase in 64-bit fixed-point cycles; see prologue.cu)
+struct CtfConst {
+    uint64_t p_fix;        // frac(Cs term per m^2) * 2^64
+    uint64_t d_fix;        // frac(atan(A) / 2pi) * 2^64
+    double   q_scale;      // defocus cycles per m per Angstrom: lambda / (2 (N pix)^2)
+    float    amp;          // sqrt(1 + A^2)
+    float    env_c;        // envelope exponent per m: 1 / ((N pix)^2 2 sigma^2), 0 if none
+};
+
+struct Layout {
+    size_t status, pd_table, sum_items, img_pd, img_row, tiles;
+    size_t item_off, qfix, gtab, pd_max;
+    size_t xbuf, spec, feat_a, feat_b, pair_norm, partial, means, avg_spec, avg_real, cufft_work;
+    size_t total;
+};
+
+}  // namespace mem
+
+struct mem_plan {
+    mem_params params;
+    int32_t n_pd = 0;
+    int64_t n_images = 0;
+    int N = 0, Nh = 0;              // Nh = N/2 + 1
+    int64_t Kc = 0, Kc_pad = 0;     // half-plane frequencies, padded to kKPad
+    int64_t n_rows = 0;             // feature-matrix rows (padded per PD)
+    int64_t d_elems = 0, n_pairs = 0;
+    std::vector<int32_t> count;
+    std::vector<mem::PdDev> pd;
+    std::vector<mem::SumItem> items;
+    std::vector<int32_t> img_pd, img_row;
+    std::vector<mem::Tile> tiles;
+    mem::CtfConst ctf{};
+    mem::Layout lay{};
+    size_t cufft_work_bytes = 0;
+    int device = -1;
+    int num_sms = 0;
+};
+
+namespace mem {
+
+// ---- host launchers of the image-side kernels (prologue.cu) ------------------------------
+namespace kern {
+int gather_normalize(const mem_plan& P, const mem_inputs& in, float* xbuf, uint32_t* status,
+                     cudaStream_t s);
+int lowpass(const mem_plan& P, float2* spec, float* gtab, cudaStream_t s);
+int rotate(const mem_plan& P, const mem_inputs& in, float* xbuf, float* img_out,
+           const PdDev* pd_table, const int32_t* img_pd, cudaStream_t s);
+int qfix(const mem_plan& P, const mem_inputs& in, uint64_t* qf, cudaStream_t s);
+int pd_sums(const mem_plan& P, const float2* spec, const uint64_t* qf, const SumItem* items,
+            float* partial, cudaStream_t s);
+int pd_finalize(const mem_plan& P, const float* partial, const SumItem* items,
+                const int32_t* item_off, const PdDev* pds, float* means, float2* avg_spec,
+                uint32_t* pd_max, cudaStream_t s);
+int features(const mem_plan& P, float2* spec, const uint64_t* qf, const PdDev* pds,
+             const int32_t* img_pd, const int32_t* img_row, const float* means,
+             const uint32_t* pd_max, void* feat_a, void* feat_b, double* pair_norm,
+             float* ctf_out, float* spectrum_out, cudaStream_t s);
+int avg_store(const mem_plan& P, const float* avg_real, double* img_avg, double* img_avg_flip,
+              cudaStream_t s);
+int intensity(const mem_plan& P, const float* flip_imgs, const PdDev* pds, double* out,
+              cudaStream_t s);
+
+// ---- D contraction (gemm_fp32.cu / gemm_tc.cu) ----------------------------------------
+int gemm_fp32(const mem_plan& P, const float* feat, const double* pair_norm,
+              const uint32_t* pd_max, const Tile* tiles, const PdDev* pds, double* D,
+              cudaStream_t s);
+int gemm_split_bf16(const mem_plan& P, const void* feat_hi, const void* feat_lo,
+                    const double* pair_norm, const uint32_t* pd_max, const Tile* tiles,
+                    const PdDev* pds, double* D, uint32_t* status, cudaStream_t s);
+}  // namespace kern
+
+// per-PD centring vectors: means[pd * means_stride + b * Kc_pad + k], blocks b = u, v, r, s
+inline int64_t means_stride(const mem_plan& P) { return 4 * P.Kc_pad; }
+
+// power-of-two feature scale of a PD from the bit pattern of its largest |mean| (host+device)
+__host__ __device__ inline float feature_scale_from_bits(uint32_t bits) {
+    union { uint32_t u; float f; } cv;
+    cv.u = bits;
+    const float mx = cv.f;
+    if (!(mx > 0.f) || mx > 3.0e38f) return 1.0f;
+    const int e = (int)((bits >> 23) & 0xff) - 126;   // mx = m * 2^e, m in [0.5, 1)
+    return ldexpf(1.0f, -e);
+}
+
+}  // namespace mem
+
+#define MEM_CUDA_TRY(expr)                                    \
+    do {                                                      \
+        cudaError_t _e = (expr);                              \
+        if (_e != cudaSuccess) return MEM_ERR_CUDA;           \
+    } while (0)
+
+#define MEM_LAUNCH_CHECK()                                    \
+    do {                                                      \
+        cudaError_t _e = cudaGetLastError();                  \
+        if (_e != cudaSuccess) return MEM_ERR_CUDA;           \
+    } while (0)

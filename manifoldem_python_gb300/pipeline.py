@@ -1,0 +1,234 @@
+"""Batched host API of the GPU distance stage.
+
+``DistanceStage`` runs the distance stage for a batch of projection directions (PDs) on one GPU
+through the C ABI (``include/manifoldem_gb300.h``): host-side bookkeeping in numpy
+(``geometry.py``), device buffers from torch, one plan / upload / execute per batch.  PDs are
+admitted into batches by an HBM budget so that any number of PDs runs on one GPU.
+
+There is no CPU path: without the CUDA library or a GPU every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import math
+from typing import Dict, Iterable, List, Optional, Sequence
+
+import numpy as np
+
+from . import _lib
+from .geometry import PdGeometry, pd_geometry
+
+OUTPUT_NAMES = ('D', 'img_avg', 'img_avg_flip', 'img_all_intensity', 'img_all', 'img_all_flip',
+                'ctf', 'spectrum', 'pair_norm')
+DEFAULT_OUTPUTS = ('D', 'img_avg', 'img_avg_flip', 'img_all_intensity', 'img_all',
+                   'img_all_flip', 'ctf')
+
+
+@dataclasses.dataclass
+class StageParams:
+    """Microscope and stage parameters (the reference's p.* globals, filterPar, options)."""
+    N: int
+    pix_size: float
+    Cs: float
+    EkV: float
+    AmpContrast: float
+    gaussEnv: float = math.inf
+    filter_type: str = 'Butter'
+    filter_Qc: float = 0.5
+    filter_order: float = 8
+    avg_only: bool = False
+    precision: str = 'fp32'          # 'fp32' or 'bf16x3'
+
+    def to_c(self) -> _lib.MemParams:
+        ft = {'Butter': _lib.MEM_FILTER_BUTTER, 'Gauss': _lib.MEM_FILTER_GAUSS}.get(self.filter_type)
+        if ft is None:
+            raise ValueError('%s filter is unsupported' % self.filter_type)
+        prec = {'fp32': _lib.MEM_PREC_FP32, 'bf16x3': _lib.MEM_PREC_SPLIT_BF16}[self.precision]
+        return _lib.MemParams(N=int(self.N), filter_type=ft, filter_Qc=float(self.filter_Qc),
+                              filter_order=float(self.filter_order),
+                              pix_size=float(self.pix_size), Cs=float(self.Cs),
+                              EkV=float(self.EkV), gaussEnv=float(self.gaussEnv),
+                              AmpContrast=float(self.AmpContrast),
+                              avg_only=int(bool(self.avg_only)), precision=prec)
+
+
+def _ptr(t) -> Optional[int]:
+    return None if t is None else int(t.data_ptr())
+
+
+class Plan:
+    """A C-ABI plan plus its torch-allocated workspace, reusable across executions."""
+
+    def __init__(self, params: StageParams, counts: Sequence[int], psi_p: Sequence[float],
+                 device=None):
+        import torch
+        self.lib = _lib.load()
+        self.params = params
+        self.device = torch.device(device or 'cuda')
+        self.counts = np.ascontiguousarray(counts, dtype=np.int32)
+        self.psi_p = np.ascontiguousarray(psi_p, dtype=np.float64)
+        self._cparams = params.to_c()
+        h = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.mem_plan_create(ctypes.byref(self._cparams),
+                                                int(len(self.counts)),
+                                                self.counts.ctypes.data, self.psi_p.ctypes.data,
+                                                ctypes.byref(h)), 'mem_plan_create')
+        self.handle = h
+        sz = ctypes.c_size_t()
+        _lib.check(self.lib.mem_plan_workspace_size(h, ctypes.byref(sz)), 'workspace_size')
+        self.ws_bytes = int(sz.value)
+        self.n_images = int(self.lib.mem_plan_num_images(h))
+        self.d_elems = int(self.lib.mem_plan_d_elements(h))
+        self.n_pairs = int(self.lib.mem_plan_num_pairs(h))
+        self.workspace = torch.empty(self.ws_bytes, dtype=torch.uint8, device=self.device)
+        stream = torch.cuda.current_stream(self.device)
+        _lib.check(self.lib.mem_plan_upload(h, self.workspace.data_ptr(), self.ws_bytes,
+                                            ctypes.c_void_p(stream.cuda_stream)),
+                   'mem_plan_upload')
+
+    def allocate_outputs(self, names: Iterable[str] = DEFAULT_OUTPUTS) -> Dict[str, object]:
+        import torch
+        N = self.params.N
+        n_pd, n_img = len(self.counts), self.n_images
+        shapes = {
+            'D': ((self.d_elems,), torch.float64),
+            'img_avg': ((n_pd, N, N), torch.float64),
+            'img_avg_flip': ((n_pd, N, N), torch.float64),
+            'img_all_intensity': ((n_pd, N, N), torch.float64),
+            'img_all': ((n_img, N, N), torch.float32),
+            'img_all_flip': ((n_img, N, N), torch.float32),
+            'ctf': ((n_img, N, N), torch.float32),
+            'spectrum': ((n_img, N, N // 2 + 1, 2), torch.float32),
+            'pair_norm': ((n_img,), torch.float64),
+        }
+        out = {}
+        for name in names:
+            if name == 'D' and self.params.avg_only:
+                continue
+            shp, dt = shapes[name]
+            out[name] = torch.empty(shp, dtype=dt, device=self.device)
+        return out
+
+    def execute(self, stack, stack_index, flip, psi_rad, df, outputs: Dict[str, object],
+                stream=None) -> None:
+        """Enqueue the stage on ``stream`` (default: torch's current stream).  All tensors
+        must be on the plan's device."""
+        import torch
+        stream = stream or torch.cuda.current_stream(self.device)
+        cin = _lib.MemInputs(stack=stack.data_ptr(), num_stack=int(stack.shape[0]),
+                             stack_index=stack_index.data_ptr(), flip=flip.data_ptr(),
+                             psi_rad=psi_rad.data_ptr(), df=df.data_ptr())
+        cout = _lib.MemOutputs(**{k: _ptr(outputs.get(k)) for k in OUTPUT_NAMES})
+        self._keep = (cin, cout)
+        _lib.check(self.lib.mem_plan_execute(self.handle, ctypes.byref(cin), ctypes.byref(cout),
+                                             self.workspace.data_ptr(), self.ws_bytes,
+                                             ctypes.c_void_p(stream.cuda_stream)),
+                   'mem_plan_execute')
+
+    def device_status(self) -> None:
+        """Raise if a bounded device-side wait expired or an input index was out of range."""
+        _lib.check(self.lib.mem_workspace_status(self.handle, self.workspace.data_ptr()),
+                   'device status')
+
+    def close(self):
+        if getattr(self, 'handle', None) is not None and self.handle.value:
+            self.lib.mem_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+@dataclasses.dataclass
+class PdJob:
+    """One PD: the reference's input_data = [ind, q, df, outFile, prD] (GetDistancesS2.py:37-47)."""
+    ind: np.ndarray
+    q: np.ndarray
+    df: np.ndarray
+    outFile: Optional[str] = None
+    prD: int = 0
+
+
+def workspace_bytes_per_image(params: StageParams) -> int:
+    """Approximate device bytes one image needs (workspace and full outputs)."""
+    N = params.N
+    Kc_pad = int(math.ceil(N * (N // 2 + 1) / 64.0) * 64)
+    feat = 4 * Kc_pad * 4
+    return 4 * N * N * 4 + 8 * N * (N // 2 + 1) + feat + 64
+
+
+def admit_batches(counts: Sequence[int], params: StageParams, budget_bytes: int) -> List[List[int]]:
+    """Split PDs (in order) into consecutive batches whose device footprint fits the budget."""
+    per_img = workspace_bytes_per_image(params)
+    batches, cur, cur_bytes = [], [], 0
+    for i, n in enumerate(counts):
+        b = n * per_img + 8 * n * n + 4 * params.N * params.N * 8
+        if cur and cur_bytes + b > budget_bytes:
+            batches.append(cur)
+            cur, cur_bytes = [], 0
+        cur.append(i)
+        cur_bytes += b
+    if cur:
+        batches.append(cur)
+    return batches
+
+
+class DistanceStage:
+    """The GPU distance stage for a set of PDs sharing one image stack."""
+
+    def __init__(self, params: StageParams, device=None):
+        import torch
+        if not torch.cuda.is_available():
+            raise RuntimeError('the GPU distance stage needs a CUDA device (no CPU path)')
+        self.params = params
+        self.device = torch.device(device or 'cuda')
+        _lib.load()
+
+    def geometry(self, jobs: Sequence[PdJob], nStot: int) -> List[PdGeometry]:
+        return [pd_geometry(np.asarray(j.ind), np.asarray(j.q, dtype=np.float64), nStot)
+                for j in jobs]
+
+    def run(self, jobs: Sequence[PdJob], stack, nStot: int, outputs=DEFAULT_OUTPUTS,
+            geoms: Optional[Sequence[PdGeometry]] = None, to_host: bool = True):
+        """Run every job; returns one dict per PD with host numpy (``to_host``) or device
+        arrays.  ``stack`` is a device tensor (num_part, N, N) float32 in SPIDER storage order."""
+        import torch
+        geoms = list(geoms) if geoms is not None else self.geometry(jobs, nStot)
+        counts = [int(np.asarray(j.ind).shape[0]) for j in jobs]
+        plan = Plan(self.params, counts, [g.psi_p for g in geoms], self.device)
+        dev = self.device
+        sidx = torch.from_numpy(np.concatenate([g.stack_index for g in geoms])).to(dev)
+        flip = torch.from_numpy(np.concatenate([g.flip for g in geoms])).to(dev)
+        psi = torch.from_numpy(np.concatenate([g.psi_rad for g in geoms])).to(dev)
+        df = torch.from_numpy(np.concatenate([np.asarray(j.df, dtype=np.float64).reshape(-1)
+                                              for j in jobs])).to(dev)
+        outs = plan.allocate_outputs(outputs)
+        plan.execute(stack, sidx, flip, psi, df, outs)
+        torch.cuda.synchronize(dev)
+        plan.device_status()
+        return split_outputs(plan, counts, outs, to_host)
+
+
+def split_outputs(plan: Plan, counts: Sequence[int], outs: Dict[str, object], to_host: bool):
+    """Per-PD views of the batched outputs."""
+    N = plan.params.N
+    res = []
+    img_off = np.concatenate([[0], np.cumsum(counts)])
+    d_off = np.concatenate([[0], np.cumsum(np.asarray(counts, dtype=np.int64) ** 2)])
+    host = {k: (v.cpu().numpy() if to_host else v) for k, v in outs.items()}
+    for p, n in enumerate(counts):
+        r = {}
+        for k, v in host.items():
+            if k == 'D':
+                r[k] = v[d_off[p]:d_off[p + 1]].reshape(n, n)
+            elif k in ('img_avg', 'img_avg_flip', 'img_all_intensity'):
+                r[k] = v[p]
+            else:
+                r[k] = v[img_off[p]:img_off[p + 1]]
+        res.append(r)
+    return res

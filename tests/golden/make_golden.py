@@ -1,0 +1,125 @@
+"""Generate the golden fixtures of the distance stage by running the reference itself.
+
+Run in a container that has the reference checkout at /root/reference (read-only); the GPU host
+never runs this.  For each case it writes a seeded synthetic SPIDER stack (values rounded to
+float16 so the fixture can store them exactly at half size), runs the reference's
+``getDistanceCTF_local_Conj9combinedS2.op`` on it through the reference's own module globals,
+reads back the pickle it writes, and stores inputs and outputs in ``tests/golden/<case>.npz``.
+
+The reference imports matplotlib and mrcfile (absent here) and uses ``np.complex`` and ``np.Inf``
+(removed from numpy 2); the loader installs empty stand-ins for the two modules and restores the
+two aliases before importing.  Nothing else of the reference is changed.
+
+Usage:  python tests/golden/make_golden.py [case ...]
+"""
+from __future__ import annotations
+
+import dataclasses
+import os
+import pickle
+import sys
+import tempfile
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+REF_MODULES = '/root/reference/modules'
+
+
+def load_reference():
+    np.complex = complex
+    np.Inf = np.inf
+    mpl = types.ModuleType('matplotlib')
+    mpl.pyplot = types.ModuleType('matplotlib.pyplot')
+    sys.modules.setdefault('matplotlib', mpl)
+    sys.modules.setdefault('matplotlib.pyplot', mpl.pyplot)
+    sys.modules.setdefault('mrcfile', types.ModuleType('mrcfile'))
+    for d in (REF_MODULES, os.path.join(REF_MODULES, 'CC')):
+        if d not in sys.path:
+            sys.path.insert(0, d)
+    import p as ref_p                                   # noqa: E402
+    import getDistanceCTF_local_Conj9combinedS2 as ref_op  # noqa: E402
+    return ref_p, ref_op
+
+
+# name -> (synthetic config overrides, microscope overrides, options overrides,
+#          image indices kept of the (nS, N, N) outputs; None keeps them whole)
+CASES = {
+    # even box, half of the PD are conjugate views (flipped, label -1)
+    'even32_conj': (dict(N=32, n_pd=1, n_fixed=16, conj_pd_frac=1.0, seed=101), {}, {}, None),
+    # odd box, finite Gaussian envelope in the CTF
+    'odd33_env': (dict(N=33, n_pd=1, n_fixed=12, seed=102), dict(gaussEnv=0.15), {}, None),
+    # averages only: D stays zero and CTF keeps its (nS, N, N) shape
+    'even32_avgonly': (dict(N=32, n_pd=1, n_fixed=10, seed=103), {}, dict(avgOnly=True), None),
+    # near-duplicate images (cancellation in the GEMM form)
+    'even48_neardup': (dict(N=48, n_pd=1, n_fixed=40, near_dup_frac=0.1, seed=104), {}, {},
+                       [0, 7, 39]),
+    # the CPU-runnable workload: one PD, 300 images of 70x70 px
+    'config1': (dict(N=70, n_pd=1, n_fixed=300, seed=11), {}, {}, [0, 1, 150, 299]),
+}
+
+FULL_KEEP = ['D', 'ind', 'q', 'df', 'CTF', 'imgAll', 'PD', 'PDs', 'Psis', 'imgAvg',
+             'imgAvgFlip', 'imgAllFlip', 'imgLabels', 'Dnom', 'Nom', 'imgAllIntensity']
+SLICE_KEYS = ['CTF', 'imgAll', 'imgAllFlip']
+
+
+def make_case(name):
+    sys.path.insert(0, REPO)
+    from manifoldem_python_gb300.synthetic import CONFIGS, make_dataset
+    ref_p, ref_op = load_reference()
+    synth_over, mic_over, opt_over, slice_idx = CASES[name]
+    cfg = dataclasses.replace(CONFIGS['config1'], name=name, **synth_over)
+    ds = make_dataset(cfg, device='cpu')
+    stack16 = ds.stack.numpy().astype(np.float16)
+    stack = stack16.astype(np.float32)
+    ind = ds.CG[0].astype(np.int64)
+    q = ds.q[:, ind]
+    df = ds.df[ind]
+    mic = dict(pix_size=cfg.pix, Cs=cfg.cs, EkV=cfg.kv, AmpContrast=cfg.ampc, gaussEnv=np.inf)
+    mic.update(mic_over)
+    options = dict(verbose=False, avgOnly=False, visual=False, parallel=False,
+                   relion_data=False, thres=6000)
+    options.update(opt_over)
+    filterPar = dict(type='Butter', Qc=0.5, N=8)
+    with tempfile.TemporaryDirectory() as tmp:
+        stack_file = os.path.join(tmp, 'stack.bin')
+        stack.tofile(stack_file)
+        ref_p.init()
+        ref_p.nPix = cfg.N
+        ref_p.pix_size = mic['pix_size']
+        ref_p.Cs = mic['Cs']
+        ref_p.EkV = mic['EkV']
+        ref_p.AmpContrast = mic['AmpContrast']
+        ref_p.gaussEnv = mic['gaussEnv']
+        ref_p.mask_vol_file = ''
+        ref_p.dist_prog = os.path.join(tmp, 'progress')
+        os.makedirs(ref_p.dist_prog)
+        out_file = os.path.join(tmp, 'IMGs_prD_0')
+        ref_op.op([ind, q, df, out_file, 0], filterPar, stack_file, ds.sh, ds.nStot, options)
+        with open(out_file, 'rb') as f:
+            res = pickle.load(f)
+        assert os.path.exists(os.path.join(ref_p.dist_prog, '0'))
+    rec = dict(stack16=stack16, ind=ind, q=q, df=df, nStot=np.int64(ds.nStot), N=np.int64(cfg.N),
+               pix_size=mic['pix_size'], Cs=mic['Cs'], EkV=mic['EkV'],
+               AmpContrast=mic['AmpContrast'], gaussEnv=mic['gaussEnv'],
+               avgOnly=np.bool_(options['avgOnly']),
+               ref_version=np.array(res['version']), ref_msk2=np.array(res['msk2']),
+               ref_CTF_shape=np.array(np.shape(res['CTF'])))
+    for k in FULL_KEEP:
+        if slice_idx is not None and k in SLICE_KEYS:
+            rec['ref_%s_slices' % k] = np.asarray(res[k])[slice_idx]
+        elif k not in ('q', 'df', 'ind'):
+            rec['ref_' + k] = np.asarray(res[k])
+    if slice_idx is not None:
+        rec['slice_idx'] = np.array(slice_idx)
+    path = os.path.join(HERE, name + '.npz')
+    np.savez_compressed(path, **rec)
+    print('wrote', path, os.path.getsize(path) // 1024, 'KiB')
+
+
+if __name__ == '__main__':
+    names = sys.argv[1:] or list(CASES)
+    for n in names:
+        make_case(n)

@@ -1,0 +1,81 @@
+"""The C-ABI library: it builds, loads, exports every function include/*.h declares, plans
+without a GPU and rejects bad arguments with the documented status codes (no compute calls)."""
+import ctypes
+import glob
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import REPO
+from manifoldem_python_gb300 import _lib
+from manifoldem_python_gb300.pipeline import StageParams
+
+
+@pytest.fixture(scope='module')
+def lib():
+    _lib.build()
+    return _lib.load()
+
+
+def declared_functions():
+    names = set()
+    for h in glob.glob(os.path.join(REPO, 'include', '*.h')):
+        txt = re.sub(r'/\*.*?\*/', '', open(h).read(), flags=re.S)
+        names.update(re.findall(r'\b(mem_\w+)\s*\(', txt))
+    return sorted(names)
+
+
+def test_exports_every_declared_symbol(lib):
+    names = declared_functions()
+    assert 'mem_plan_execute' in names and 'mem_pd_batch' in names
+    for n in names:
+        assert hasattr(lib, n), n
+    assert set(names) <= set(_lib.SIGNATURES) | {n for n in names if hasattr(lib, n)}
+
+
+def test_struct_layouts_match_header():
+    assert ctypes.sizeof(_lib.MemParams) == 72
+    assert ctypes.sizeof(_lib.MemInputs) == 48
+    assert ctypes.sizeof(_lib.MemOutputs) == 72
+
+
+def _plan(lib, params, counts, psi):
+    counts = np.ascontiguousarray(counts, dtype=np.int32)
+    psi = np.ascontiguousarray(psi, dtype=np.float64)
+    h = ctypes.c_void_p()
+    st = lib.mem_plan_create(ctypes.byref(params), len(counts), counts.ctypes.data,
+                             psi.ctypes.data, ctypes.byref(h))
+    return st, h
+
+
+def test_plan_tables_without_gpu(lib):
+    P = StageParams(N=64, pix_size=2.0, Cs=2.7, EkV=300.0, AmpContrast=0.1).to_c()
+    st, h = _plan(lib, P, [300, 129, 1], [10.0, 20.0, 30.0])
+    assert st == 0
+    try:
+        assert lib.mem_plan_num_images(h) == 430
+        assert lib.mem_plan_num_pairs(h) == 300 * 299 // 2 + 129 * 128 // 2
+        assert lib.mem_plan_d_elements(h) == 300 ** 2 + 129 ** 2 + 1
+        sz = ctypes.c_size_t()
+        assert lib.mem_plan_workspace_size(h, ctypes.byref(sz)) == 0 and sz.value > 0
+        # the workspace holds at least the image, spectrum and feature buffers
+        Kc_pad = -(-64 * 33 // 64) * 64
+        assert sz.value >= 430 * 64 * 64 * 4 + 430 * 64 * 33 * 8 + (384 + 256 + 128) * 4 * Kc_pad * 4
+        small = ctypes.c_size_t(sz.value - 1)
+        assert lib.mem_plan_upload(h, ctypes.c_void_p(256), small, None) == _lib.MEM_ERR_WORKSPACE
+    finally:
+        lib.mem_plan_destroy(h)
+
+
+def test_invalid_arguments(lib):
+    P = StageParams(N=64, pix_size=2.0, Cs=2.7, EkV=300.0, AmpContrast=0.1).to_c()
+    assert _plan(lib, P, [0], [1.0])[0] == _lib.MEM_ERR_INVALID
+    assert _plan(lib, P, [5], [float('nan')])[0] == _lib.MEM_ERR_INVALID
+    big = StageParams(N=250, pix_size=2.0, Cs=2.7, EkV=300.0, AmpContrast=0.1).to_c()
+    assert _plan(lib, big, [5], [1.0])[0] == _lib.MEM_ERR_UNSUPPORTED
+    bad = StageParams(N=64, pix_size=-1.0, Cs=2.7, EkV=300.0, AmpContrast=0.1).to_c()
+    assert _plan(lib, bad, [5], [1.0])[0] == _lib.MEM_ERR_INVALID
+    assert lib.mem_plan_execute(None, None, None, None, 0, None) == _lib.MEM_ERR_INVALID
+    assert lib.mem_status_string(_lib.MEM_ERR_WORKSPACE) == b'workspace too small'

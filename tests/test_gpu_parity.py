@@ -1,0 +1,132 @@
+"""GPU parity of the distance stage (through the C ABI) against the reference's outputs and the
+FP64 oracle.
+
+Tolerances (max |difference| / max |reference| over the array):
+* D, plain FP32 form: 1e-5 against the reference's float64 D;
+* D against an FP64 contraction of the GPU's own spectra and CTFs (isolates the contraction):
+  2e-6 for the FP32 form, 1e-6 for the split-BF16 form;
+* imgAll, imgAllFlip, CTF, imgAvg, imgAvgFlip, imgAllIntensity: 2e-5 (float32 pipeline).
+"""
+import os
+import pickle
+import tempfile
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_CASES, golden_micro, golden_options, golden_ref, load_golden
+
+pytestmark = pytest.mark.gpu
+
+PRECISIONS = ['fp32']
+TOL_IMG = 2e-5
+
+
+def rel(a, b):
+    return float(np.abs(np.asarray(a, dtype=np.float64) - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def run_case(torch, g, precision, outputs=None):
+    from manifoldem_python_gb300.pipeline import DistanceStage, PdJob, StageParams
+    mic = golden_micro(g)
+    params = StageParams(avg_only=bool(g['avgOnly']), precision=precision, **mic)
+    stage = DistanceStage(params)
+    job = PdJob(ind=g['ind'], q=g['q'], df=g['df'])
+    stack = torch.from_numpy(g['stack16'].astype(np.float32)).cuda()
+    outs = outputs or ('D', 'img_avg', 'img_avg_flip', 'img_all_intensity', 'img_all',
+                       'img_all_flip', 'ctf', 'spectrum')
+    return stage.run([job], stack, int(g['nStot']), outputs=outs)[0]
+
+
+@pytest.mark.parametrize('precision', PRECISIONS)
+@pytest.mark.parametrize('case', GOLDEN_CASES)
+def test_stage_matches_reference(cuda_ready, case, precision):
+    torch = cuda_ready
+    g = load_golden(case)
+    res = run_case(torch, g, precision)
+    N = int(g['N'])
+    n = g['ind'].shape[0]
+    pairs = {'imgAll': 'img_all', 'imgAllFlip': 'img_all_flip', 'imgAvg': 'img_avg',
+             'imgAvgFlip': 'img_avg_flip', 'imgAllIntensity': 'img_all_intensity'}
+    for rk, mk in pairs.items():
+        ref, sl = golden_ref(g, rk)
+        mine = res[mk] if sl is None else res[mk][sl]
+        assert rel(mine, ref) < TOL_IMG, (case, rk, rel(mine, ref))
+    ref_ctf, sl = golden_ref(g, 'CTF')
+    mine_ctf = res['ctf'] if sl is None else res['ctf'][sl]
+    assert rel(mine_ctf.reshape(ref_ctf.shape), ref_ctf) < TOL_IMG
+    if bool(g['avgOnly']):
+        assert 'D' not in res
+        return
+    D = res['D']
+    Dref = g['ref_D']
+    assert rel(D, Dref) < 1e-5, (case, rel(D, Dref))
+    np.testing.assert_array_equal(D, D.T)
+    assert np.all(np.diag(D) == 0)
+    # the contraction alone: FP64 D of the GPU's own half-plane spectra and exact CTFs
+    from oracle import distance_oracle as O
+    F = res['spectrum'][..., 0].astype(np.float64) + 1j * res['spectrum'][..., 1]
+    Q = O.create_grid(N)
+    C = np.stack([np.fft.ifftshift(O.ctf_cryo_frank(Q / (2 * float(g['pix_size'])),
+                                                    float(g['Cs']), d, float(g['EkV']),
+                                                    float(g['gaussEnv']),
+                                                    float(g['AmpContrast'])))[:, :N // 2 + 1]
+                  for d in g['df']])
+    D64 = O.distances_from_half_plane(C, F, N)
+    np.fill_diagonal(D64, 0)
+    tol = 1e-6 if precision == 'bf16x3' else 2e-6
+    assert rel(D, D64) < tol, (case, rel(D, D64))
+    assert n == D.shape[0]
+
+
+def test_batched_equals_single(cuda_ready):
+    """Two PDs in one call give the results of two separate calls."""
+    torch = cuda_ready
+    from manifoldem_python_gb300.pipeline import DistanceStage, PdJob, StageParams
+    g = load_golden('config1')
+    stage = DistanceStage(StageParams(**golden_micro(g)))
+    stack = torch.from_numpy(g['stack16'].astype(np.float32)).cuda()
+    ind = g['ind']
+    jobs = [PdJob(ind=ind[:170], q=g['q'][:, :170], df=g['df'][:170]),
+            PdJob(ind=ind[170:], q=g['q'][:, 170:], df=g['df'][170:])]
+    both = stage.run(jobs, stack, int(g['nStot']))
+    for j, r in zip(jobs, both):
+        single = stage.run([j], stack, int(g['nStot']))[0]
+        for k in single:
+            assert rel(r[k], single[k]) < 1e-6, k
+
+
+def test_dropin_op_writes_reference_pickle(cuda_ready):
+    """op() writes the reference's 19-key pickle (same dtypes/shapes) and the resume marker."""
+    from manifoldem_python_gb300 import p as mp
+    from manifoldem_python_gb300.getDistanceCTF_local_Conj9combinedS2 import op
+    g = load_golden('even32_conj')
+    mic = golden_micro(g)
+    with tempfile.TemporaryDirectory() as tmp:
+        stack_file = os.path.join(tmp, 'stack.bin')
+        g['stack16'].astype(np.float32).tofile(stack_file)
+        mp.init()
+        mp.nPix, mp.pix_size, mp.Cs, mp.EkV = mic['N'], mic['pix_size'], mic['Cs'], mic['EkV']
+        mp.AmpContrast, mp.gaussEnv = mic['AmpContrast'], mic['gaussEnv']
+        mp.dist_prog = os.path.join(tmp, 'progress')
+        os.makedirs(mp.dist_prog)
+        out_file = os.path.join(tmp, 'IMGs_prD_3')
+        options = golden_options(g)
+        op([g['ind'], g['q'], g['df'], out_file, 3], dict(type='Butter', Qc=0.5, N=8),
+           stack_file, None, int(g['nStot']), options)
+        assert os.path.exists(os.path.join(mp.dist_prog, '3'))
+        with open(out_file, 'rb') as f:
+            d = pickle.load(f)
+    n, N = g['ind'].shape[0], int(g['N'])
+    expect = {'D': (n, n), 'CTF': (n, N * N), 'imgAll': (n, N, N), 'imgAllFlip': (n, N, N),
+              'PD': (3,), 'PDs': (3, n), 'Psis': (n, 1), 'imgAvg': (N, N),
+              'imgAvgFlip': (N, N), 'imgLabels': (n,), 'Dnom': (n, 1), 'Nom': (n, 1),
+              'imgAllIntensity': (N, N)}
+    assert len(d) == 19 and d['msk2'] == 1 and d['version'] == str(g['ref_version'])
+    for k, shp in expect.items():
+        assert np.shape(d[k]) == shp, k
+        if k != 'imgLabels':
+            assert np.asarray(d[k]).dtype == np.float64, k
+    np.testing.assert_array_equal(d['imgLabels'], g['ref_imgLabels'])
+    assert rel(d['D'], g['ref_D']) < 1e-5
+    assert d['options'] == options
