@@ -1,0 +1,468 @@
+"""Benchmark of the GPU distance stage: all-PD CTF-distance pairs/s on one GB300.
+
+Workload (default, --config config4): 800 projection directions (PDs) of 128x128 px images,
+particles per PD log-normal (median 400, sigma 0.6, clipped to 100-3000), 10% of PDs made of
+conjugate views, seeded synthetic data (no public dataset is named; the reference's demo stack is
+absent).  One step = the whole distance stage for every PD (gather, normalisation, low-pass,
+mask, two spline rotations, CTF, spectra, Wiener / phase-flip averages, imgAllIntensity, D),
+i.e. ``mem_plan_execute`` over all 800 PDs.  Pickle writing is not part of a step.
+
+Printed JSON line (rank 0):
+  value     pairs/s with inputs resident in HBM (timed on the stream with CUDA events)
+  e2e       the same through the C-ABI call with host buffers: pinned-host stack and per-image
+            metadata copied in, D and the averages copied out, inside the timed region
+  roofline  the dominant phase of a step, timed live with CUDA events
+  cpu_baseline  the FP64 CPU port of the reference (oracle/) on a bounded sample of PDs,
+            extrapolated to the whole workload by a fitted t(n) = a n + b n^2
+``--impl reference`` times that CPU port alone (the reference itself is Python and cannot run on
+the GPU host) on the same workload and prints the same line with "impl": "reference".
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+L2_BYTES = 129 * 1024 * 1024
+
+
+def load_peaks():
+    path = os.path.join(HERE, 'MEASURED_PEAKS.json')
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return dict(hbm=d['hbm_gbs'], bf16=d['bf16_tflops'],
+                    bf16_sust=d['bf16_tflops_sustained'], src='measured')
+    return dict(hbm=6800.0, bf16=1900.0, bf16_sust=1700.0, src='fallback')
+
+
+class ClockSampler:
+    """nvidia-smi SM clock / throttle sampling while the timed region runs."""
+    Q = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,'
+         'clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,'
+         'clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ['nvidia-smi', '-i', str(self.gpu), '--query-gpu=' + self.Q,
+                 '--format=csv,noheader,nounits', '-lms', '100'],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(',')]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[4:8]):
+                if v.lower() == 'active':
+                    reasons.add(nm)
+        return {'sm_mhz': statistics.median(sm) if sm else None, 'sm_max_mhz': mx,
+                'reasons': sorted(reasons), 'samples': len(sm)}
+
+
+# ------------------------------------------------------------------------------- CPU side
+def _oracle_pd(args):
+    """One PD through the FP64 CPU port; returns (n, seconds)."""
+    import numpy as _np
+    from oracle import distance_oracle as O
+    stack, ind, q, df, nStot, mic = args
+    t0 = time.perf_counter()
+    O.pd_op(ind, q, df, stack, nStot, **mic)
+    return int(ind.shape[0]), time.perf_counter() - t0
+
+
+def cpu_sample_tasks(ds, pds, mic):
+    """Compact per-PD inputs (stack of the PD's images, indices remapped) for the CPU port."""
+    tasks = []
+    stack_all = ds.stack
+    for p in pds:
+        ind = np.asarray(ds.CG[p])
+        conj = ind >= ds.num_part
+        sidx = np.where(conj, ind - ds.num_part, ind)
+        n = ind.size
+        imgs = stack_all[sidx].cpu().numpy() if hasattr(stack_all, 'cpu') else stack_all[sidx]
+        new_ind = np.arange(n) + np.where(conj, n, 0)
+        tasks.append((imgs, new_ind, ds.q[:, ind], ds.df[ind], 2 * n, mic))
+    return tasks
+
+
+def run_cpu_tasks(tasks, cores):
+    import multiprocessing as mp
+    os.environ.setdefault('OMP_NUM_THREADS', '1')
+    os.environ.setdefault('OPENBLAS_NUM_THREADS', '1')
+    os.environ.setdefault('MKL_NUM_THREADS', '1')
+    ctx = mp.get_context('spawn')
+    t0 = time.perf_counter()
+    with ctx.Pool(processes=cores) as pool:
+        res = pool.map(_oracle_pd, tasks, chunksize=1)
+    return res, time.perf_counter() - t0
+
+
+def extrapolate_pairs_per_s(res, wall, counts, cores):
+    """Fit per-PD CPU time t(n) = a n + b n^2 on the sample and predict the wall time of the
+    whole workload on `cores` workers (perfect packing); returns pairs/s."""
+    n = np.array([r[0] for r in res], dtype=np.float64)
+    t = np.array([r[1] for r in res], dtype=np.float64)
+    A = np.vstack([n, n * n]).T
+    coef, *_ = np.linalg.lstsq(A, t, rcond=None)
+    a, b = max(coef[0], 0.0), max(coef[1], 0.0)
+    if a == 0 and b == 0:
+        a = float(np.sum(t) / np.sum(n))
+    counts = np.asarray(counts, dtype=np.float64)
+    total_t = float(np.sum(a * counts + b * counts * counts)) / cores
+    pairs = float(np.sum(counts * (counts - 1) / 2))
+    return pairs / total_t, dict(a=a, b=b, sample_pairs_per_s=float(
+        np.sum(n * (n - 1) / 2) / wall))
+
+
+def choose_sample(counts, cores, max_n):
+    """PDs at evenly spaced quantiles of the size distribution, capped at max_n particles."""
+    order = np.argsort(counts, kind='stable')
+    k = cores
+    qs = (np.arange(k) + 0.5) / k
+    pick = []
+    for qv in qs:
+        p = int(order[min(len(order) - 1, int(qv * len(order)))])
+        if counts[p] <= max_n and p not in pick:
+            pick.append(p)
+    return pick
+
+
+# ------------------------------------------------------------------------------- GPU side
+def kernels_per_execute(outputs, avg_only):
+    """Kernels of this library one mem_plan_execute launches (cuFFT kernels excluded):
+    gather_normalize, lowpass_table, lowpass_apply, rotate, qfix, pd_sums, pd_finalize,
+    features, [avg_store], [intensity], [contraction]."""
+    k = 8
+    if 'img_avg' in outputs or 'img_avg_flip' in outputs:
+        k += 1
+    if 'img_all_intensity' in outputs:
+        k += 1
+    if 'D' in outputs and not avg_only:
+        k += 1
+    return k
+
+
+def traffic_from_profiles(kernel_tag, workload):
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary, if any."""
+    path = os.path.join(HERE, 'profiles', '%s_%s.md' % (kernel_tag, workload))
+    if not os.path.exists(path):
+        return None
+    m = re.search(r'traffic_bytes_per_full_launch:\s*([0-9.eE+]+)', open(path).read())
+    return float(m.group(1)) if m else None
+
+
+def run_gpu(args, rank, world):
+    import torch
+    from manifoldem_python_gb300.pipeline import Plan, StageParams
+    from manifoldem_python_gb300.geometry import pd_geometry
+    from manifoldem_python_gb300.synthetic import CONFIGS, make_dataset
+    import dataclasses
+
+    dev = torch.device('cuda', int(os.environ.get('LOCAL_RANK', 0)))
+    torch.cuda.set_device(dev)
+    cfg = CONFIGS[args.config]
+    if args.n_pd:
+        cfg = dataclasses.replace(cfg, n_pd=args.n_pd)
+    cfg = dataclasses.replace(cfg, seed=cfg.seed + 1000 * rank)
+    t0 = time.time()
+    ds = make_dataset(cfg, device=dev)
+    torch.cuda.synchronize(dev)
+    t_gen = time.time() - t0
+    geoms = [pd_geometry(np.asarray(ind), ds.q[:, ind], ds.nStot) for ind in ds.CG]
+    counts = [int(len(ind)) for ind in ds.CG]
+    params = StageParams(N=cfg.N, pix_size=cfg.pix, Cs=cfg.cs, EkV=cfg.kv,
+                         AmpContrast=cfg.ampc, precision=args.precision)
+    plan = Plan(params, counts, [g.psi_p for g in geoms], dev)
+    outputs = tuple(args.outputs.split(','))
+    outs = plan.allocate_outputs(outputs)
+    sidx_h = np.concatenate([g.stack_index for g in geoms])
+    flip_h = np.concatenate([g.flip for g in geoms])
+    psi_h = np.concatenate([g.psi_rad for g in geoms])
+    df_h = np.concatenate([ds.df[ind] for ind in ds.CG]).astype(np.float64)
+    sidx = torch.from_numpy(sidx_h).to(dev)
+    flip = torch.from_numpy(flip_h).to(dev)
+    psi = torch.from_numpy(psi_h).to(dev)
+    dfd = torch.from_numpy(df_h).to(dev)
+    stack = ds.stack
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        plan.execute(stack, sidx, flip, psi, dfd, outs, stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize(dev)
+    plan.device_status()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev.index) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    plan.device_status()
+
+    # live phase timing of one step (CUDA events between the phases)
+    import ctypes
+    lib = plan.lib
+    lib.mem_plan_set_timing(plan.handle, 1)
+    step()
+    phase_ms = (ctypes.c_float * 9)()
+    lib.mem_plan_phase_times(plan.handle, phase_ms, 9)
+    lib.mem_plan_set_timing(plan.handle, 0)
+    phases = {lib.mem_phase_name(i).decode(): float(phase_ms[i]) for i in range(9)}
+
+    # end to end through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        pin = True
+        try:
+            stack_h = torch.empty(stack.shape, dtype=stack.dtype, pin_memory=True)
+        except RuntimeError:
+            stack_h, pin = torch.empty(stack.shape, dtype=stack.dtype), False
+        stack_h.copy_(stack)
+        meta_h = [torch.from_numpy(x).pin_memory() if pin else torch.from_numpy(x)
+                  for x in (sidx_h, flip_h, psi_h, df_h)]
+        res_names = [k for k in ('D', 'img_avg', 'img_avg_flip', 'img_all_intensity') if k in outs]
+        res_h = {k: torch.empty(outs[k].shape, dtype=outs[k].dtype, pin_memory=pin)
+                 for k in res_names}
+        h2d = stack_h.numel() * 4 + sum(m.numel() * m.element_size() for m in meta_h)
+        d2h = sum(v.numel() * v.element_size() for v in res_h.values())
+
+        def e2e_step():
+            stack.copy_(stack_h, non_blocking=True)
+            for dst, src in zip((sidx, flip, psi, dfd), meta_h):
+                dst.copy_(src, non_blocking=True)
+            plan.execute(stack, sidx, flip, psi, dfd, outs, stream)
+            for k in res_names:
+                res_h[k].copy_(outs[k], non_blocking=True)
+
+        e2e_step()
+        torch.cuda.synchronize(dev)
+        k_e2e = max(1, min(args.steps, 5))
+        t0 = time.perf_counter()
+        for _ in range(k_e2e):
+            e2e_step()
+        torch.cuda.synchronize(dev)
+        e2e_ms = (time.perf_counter() - t0) * 1000 / k_e2e
+        if world > 1:
+            t = torch.tensor([e2e_ms], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            e2e_ms = float(t.item())
+        e2e = dict(ms=e2e_ms, h2d=int(h2d), d2h=int(d2h), pinned=pin)
+        del stack_h, res_h
+    return dict(ms=ms, pairs=plan.n_pairs, n_images=plan.n_images, counts=counts,
+                phases=phases, clocks=clk.summary(), t_gen=t_gen, e2e=e2e, ds=ds, cfg=cfg,
+                kernels=kernels_per_execute(outputs, False), outputs=outputs)
+
+
+def roofline(r, args):
+    peaks = load_peaks()
+    ph = r['phases']
+    dom = max(ph, key=ph.get)
+    cfg = r['cfg']
+    N = cfg.N
+    K = 4 * N * (N // 2 + 1)
+    if dom == 'contraction':
+        flops = 2.0 * K * r['pairs']
+        ach = flops / (ph[dom] * 1e-3) / 1e12
+        peak = peaks['bf16_sust']
+        return dict(phase=dom, bound='tensor', achieved=ach, peak=peak, unit='TFLOP/s',
+                    frac=ach / peak, traffic=traffic_from_profiles('contraction_' + args.precision,
+                                                                   args.config),
+                    peak_source=peaks['src'] + ' bf16 sustained', algorithmic_flops=flops)
+    # image-side phases: algorithmic bytes per image of the phase
+    NN, Kc = N * N, N * (N // 2 + 1)
+    per_img = {'gather': 2 * 4 * NN, 'lowpass': 2 * (4 * NN + 8 * Kc), 'rotate': 4 * 4 * NN,
+               'spectrum': 4 * NN + 8 * Kc, 'sums': 8 * Kc, 'features': 8 * Kc + 16 * Kc + 8 * Kc,
+               'averages': 0, 'flip': 8 * Kc + 4 * NN, }.get(dom, 4 * NN)
+    b = per_img * r['n_images']
+    ach = b / (ph[dom] * 1e-3) / 1e9
+    return dict(phase=dom, bound='hbm', achieved=ach, peak=peaks['hbm'], unit='GB/s',
+                frac=ach / peaks['hbm'], traffic=traffic_from_profiles(dom, args.config),
+                peak_source=peaks['src'] + ' hbm', algorithmic_bytes=b)
+
+
+def cpu_baseline(args, ds, counts, cfg, steps=1, budget_s=20.0):
+    cores = os.cpu_count() or 1
+    mic = dict(N=cfg.N, pix_size=cfg.pix, Cs=cfg.cs, EkV=cfg.kv, AmpContrast=cfg.ampc)
+    pick = choose_sample(np.asarray(counts), cores, max_n=args.cpu_max_n)
+    tasks = cpu_sample_tasks(ds, pick, mic)
+    vals, walls = [], []
+    for _ in range(steps):
+        res, wall = run_cpu_tasks(tasks, cores)
+        v, fit = extrapolate_pairs_per_s(res, wall, counts, cores)
+        vals.append(v)
+        walls.append(wall)
+    sample = ('%d PDs at size quantiles (n=%s) of the %s workload, one per core, FP64 CPU port '
+              '(oracle/distance_oracle.pd_op); pairs/s extrapolated to all %d PDs with '
+              't(n)=a n + b n^2 fitted on the sample (a=%.3g s, b=%.3g s); sample wall %.1f s'
+              % (len(pick), sorted(int(counts[p]) for p in pick), args.config, len(counts),
+                 fit['a'], fit['b'], walls[-1]))
+    return dict(value=float(np.median(vals)), unit='pairs/s', cores=cores, kind='port',
+                sample=sample), walls
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=10)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    ap.add_argument('--config', default='config4')
+    ap.add_argument('--n-pd', type=int, default=0, help='override the number of PDs')
+    ap.add_argument('--precision', default='fp32', choices=['fp32', 'bf16x3'])
+    ap.add_argument('--outputs', default='D,img_avg,img_avg_flip,img_all_intensity')
+    ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--no-e2e', action='store_true')
+    ap.add_argument('--cpu-max-n', type=int, default=900)
+    args = ap.parse_args()
+
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    metric = 'all-PD CTF-distance pairs/s'
+
+    if args.impl == 'reference':
+        if rank != 0:
+            return
+        from manifoldem_python_gb300.synthetic import CONFIGS, make_dataset, particle_counts
+        import dataclasses
+        cfg = CONFIGS[args.config]
+        if args.n_pd:
+            cfg = dataclasses.replace(cfg, n_pd=args.n_pd)
+        counts = particle_counts(cfg)[:cfg.n_pd]
+        cores = os.cpu_count() or 1
+        pick = choose_sample(counts, cores, max_n=args.cpu_max_n)
+        ds = make_dataset(cfg, device='cpu', pd_select=pick)
+        mic = dict(N=cfg.N, pix_size=cfg.pix, Cs=cfg.cs, EkV=cfg.kv, AmpContrast=cfg.ampc)
+        tasks = []
+        for j, p in enumerate(pick):
+            ind = np.asarray(ds.CG[j])
+            conj = ind >= ds.num_part
+            sidx = np.where(conj, ind - ds.num_part, ind)
+            n = ind.size
+            tasks.append((ds.stack[sidx].numpy(), np.arange(n) + np.where(conj, n, 0),
+                          ds.q[:, ind], ds.df[ind], 2 * n, mic))
+        for _ in range(args.warmup):
+            run_cpu_tasks(tasks[:1], 1)
+        vals, walls = [], []
+        for _ in range(args.steps):
+            res, wall = run_cpu_tasks(tasks, cores)
+            v, fit = extrapolate_pairs_per_s(res, wall, counts, cores)
+            vals.append(v)
+            walls.append(wall)
+        v = float(np.median(vals))
+        sample = ('%d PDs at size quantiles (n=%s) of the %s workload per step, one per core, '
+                  'FP64 CPU port of the reference (oracle/); pairs/s extrapolated to all %d PDs '
+                  'by t(n)=a n + b n^2' % (len(pick), sorted(int(counts[p]) for p in pick),
+                                           args.config, len(counts)))
+        line = dict(metric=metric, value=v, unit='pairs/s', n_gpus=args.gpus, steps=args.steps,
+                    warmup=args.warmup, ms_per_step=float(np.median(walls)) * 1000,
+                    higher_is_better=True, scaling='weak', vs_baseline=None, dtype='f64',
+                    data='synthetic', impl='reference',
+                    config=dict(workload='%s: %d PDs, %dx%d px' % (args.config, len(counts),
+                                                                  cfg.N, cfg.N)),
+                    cpu_baseline=dict(value=v, unit='pairs/s', cores=cores, kind='port',
+                                      sample=sample),
+                    e2e=dict(value=v, unit='pairs/s', h2d_bytes_per_step=0,
+                             d2h_bytes_per_step=0))
+        print(json.dumps(line))
+        return
+
+    import torch
+    if world > 1:
+        torch.distributed.init_process_group('nccl')
+    r = run_gpu(args, rank, world)
+    pairs_total = r['pairs'] * world
+    value = pairs_total / (r['ms'] * 1e-3)
+    if rank != 0:
+        if world > 1:
+            torch.distributed.barrier()
+        return
+    rl = roofline(r, args)
+    cfg = r['cfg']
+    line = dict(
+        metric=metric, value=value, unit='pairs/s', n_gpus=world, steps=args.steps,
+        warmup=args.warmup, ms_per_step=r['ms'], higher_is_better=True, scaling='weak',
+        vs_baseline=None, dtype='f32' if args.precision == 'fp32' else 'bf16x3+f32acc',
+        data='synthetic (seeded generator, 3-D Gaussian-blob volume, CTF, SNR %.2g)' % cfg.snr,
+        config=dict(workload='%s: %d PDs, %dx%d px, n~lognormal(median %d), %d images, '
+                             '%d pairs per GPU' % (args.config, len(r['counts']), cfg.N, cfg.N,
+                                                   cfg.n_median, r['n_images'], r['pairs']),
+                    precision=args.precision, outputs=list(r['outputs']),
+                    l2='inputs larger than L2 (%.1f GB image stack)' % (
+                        r['ds'].stack.numel() * 4 / 1e9),
+                    parallelism='PD-sharded, one process per GPU' if world > 1 else 'single GPU'),
+        roofline=dict(bound=rl['bound'], achieved=rl['achieved'], peak=rl['peak'],
+                      unit=rl['unit'], frac=rl['frac'], traffic=rl['traffic'],
+                      kernel=rl['phase'], peak_source=rl['peak_source']),
+        phases_ms=r['phases'],
+        clocks=r['clocks'],
+        gpu_launches=r['kernels'] * args.steps,
+    )
+    if r['e2e']:
+        e = r['e2e']
+        line['e2e'] = dict(value=pairs_total / (e['ms'] * 1e-3), unit='pairs/s',
+                           h2d_bytes_per_step=e['h2d'], d2h_bytes_per_step=e['d2h'],
+                           ms_per_step=e['ms'], pinned=e['pinned'])
+    if not args.no_cpu_baseline:
+        cb, _ = cpu_baseline(args, r['ds'], r['counts'], cfg)
+        line['cpu_baseline'] = cb
+    print(json.dumps(line))
+    if world > 1:
+        torch.distributed.barrier()
+
+
+if __name__ == '__main__':
+    main()

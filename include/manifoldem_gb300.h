@@ -130,6 +130,17 @@ int mem_plan_execute(mem_plan* plan, const mem_inputs* in, const mem_outputs* ou
  * MEM_OK, or MEM_ERR_DEVICE_TIMEOUT if a bounded device-side wait gave up.                 */
 int mem_workspace_status(const mem_plan* plan, const void* workspace);
 
+/* ---- phase timing ------------------------------------------------------------------------
+ * When enabled, mem_plan_execute records CUDA events between its phases (gather, lowpass,
+ * rotate, spectrum, sums, features, averages, flip, contraction).  mem_plan_phase_times waits
+ * for the last execute's events and writes up to max_phases durations in milliseconds (phases
+ * that did not run report 0); it returns the number of phases.  Keep timing disabled while
+ * capturing a graph.                                                                        */
+#define MEM_NUM_PHASES 9
+int mem_plan_set_timing(mem_plan* plan, int enable);
+int mem_plan_phase_times(mem_plan* plan, float* ms_out, int max_phases);
+const char* mem_phase_name(int phase);
+
 /* One-shot convenience: plan, upload and execute on `stream`, then destroy the plan.
  * The workspace must be at least the size mem_plan_workspace_size reports for the same
  * arguments.                                                                               */

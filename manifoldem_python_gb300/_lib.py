@@ -136,6 +136,9 @@ SIGNATURES = {
     'mem_plan_execute': (c_int32, [c_void_p, ctypes.POINTER(MemInputs),
                                    ctypes.POINTER(MemOutputs), c_void_p, c_size_t, c_void_p]),
     'mem_workspace_status': (c_int32, [c_void_p, c_void_p]),
+    'mem_plan_set_timing': (c_int32, [c_void_p, c_int32]),
+    'mem_plan_phase_times': (c_int32, [c_void_p, ctypes.POINTER(ctypes.c_float), c_int32]),
+    'mem_phase_name': (ctypes.c_char_p, [c_int32]),
     'mem_pd_batch': (c_int32, [ctypes.POINTER(MemParams), c_int32, c_void_p, c_void_p,
                                ctypes.POINTER(MemInputs), ctypes.POINTER(MemOutputs), c_void_p,
                                c_size_t, c_void_p]),

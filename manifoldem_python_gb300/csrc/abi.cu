@@ -350,6 +350,16 @@ int mem_plan_execute(mem_plan* plan, const mem_inputs* in, const mem_outputs* ou
     cudaStream_t s = (cudaStream_t)stream;
     void* ws = workspace;
     uint32_t* status = at<uint32_t>(ws, L.status);
+    mem_plan& PM = *plan;
+    PM.timed_run = PM.timing;
+    for (bool& r : PM.phase_ran) r = false;
+    // event k marks the start of phase k; phase k ends at the next recorded event
+    auto mark = [&](int phase) -> int {
+        if (!PM.timing) return MEM_OK;
+        MEM_CUDA_TRY(cudaEventRecord(PM.ev[phase], s));
+        if (phase > 0) PM.phase_ran[phase - 1] = true;
+        return MEM_OK;
+    };
     const PdDev* pds = at<PdDev>(ws, L.pd_table);
     const int32_t* img_pd = at<int32_t>(ws, L.img_pd);
     const int32_t* img_row = at<int32_t>(ws, L.img_row);
@@ -368,16 +378,21 @@ int mem_plan_execute(mem_plan* plan, const mem_inputs* in, const mem_outputs* ou
 
     MEM_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(uint32_t) * 4, s));
     // (a2) gather, conjugate flip, normalisation
+    MEM_STEP(mark(0));
     MEM_STEP(kern::gather_normalize(P, *in, xbuf, status, s));
+    MEM_STEP(mark(1));
     // (a3) low-pass filter: R2C, multiply by G/N^2, C2R
     MEM_STEP(exec_fft(P, CUFFT_R2C, P.n_images, NN, specN, xbuf, spec, work, s));
     MEM_STEP(kern::lowpass(P, spec, at<float>(ws, L.gtab), s));
     MEM_STEP(exec_fft(P, CUFFT_C2R, P.n_images, specN, NN, spec, xbuf, work, s));
+    MEM_STEP(mark(2));
     // (a4, a6) mask and the two rotations -> imgAll
     float* img_all = out->img_all ? out->img_all : xbuf;
     MEM_STEP(kern::rotate(P, *in, xbuf, img_all, pds, img_pd, s));
+    MEM_STEP(mark(3));
     // (a8) F = fft2(imgAll)
     MEM_STEP(exec_fft(P, CUFFT_R2C, P.n_images, NN, specN, img_all, spec, work, s));
+    MEM_STEP(mark(4));
     // (a7, a9) CTF, per-PD sums, centring vectors, average spectra
     MEM_STEP(kern::qfix(P, *in, qf, s));
     float* partial = at<float>(ws, L.partial);
@@ -387,24 +402,28 @@ int mem_plan_execute(mem_plan* plan, const mem_inputs* in, const mem_outputs* ou
     uint32_t* pd_max = at<uint32_t>(ws, L.pd_max);
     MEM_STEP(kern::pd_finalize(P, partial, at<SumItem>(ws, L.sum_items),
                                at<int32_t>(ws, L.item_off), pds, means, avg_spec, pd_max, s));
+    MEM_STEP(mark(5));
     // features of D, a_i, sign(C) F, CTF output
     void* feat_a = at<char>(ws, L.feat_a);
     void* feat_b = at<char>(ws, L.feat_b);
     double* pair_norm = out->pair_norm ? out->pair_norm : at<double>(ws, L.pair_norm);
     MEM_STEP(kern::features(P, spec, qf, pds, img_pd, img_row, means, pd_max, feat_a, feat_b,
                             pair_norm, out->ctf, out->spectrum, s));
+    MEM_STEP(mark(6));
     // averages: one inverse transform per PD (linearity of the reference's per-image sums)
     float* avg_real = at<float>(ws, L.avg_real);
     if (out->img_avg || out->img_avg_flip) {
         MEM_STEP(exec_fft(P, CUFFT_C2R, 2 * P.n_pd, specN, NN, avg_spec, avg_real, work, s));
         MEM_STEP(kern::avg_store(P, avg_real, out->img_avg, out->img_avg_flip, s));
     }
+    MEM_STEP(mark(7));
     // phase-flipped images and their mean intensity
     if (out->img_all_flip || out->img_all_intensity) {
         float* flip_imgs = out->img_all_flip ? out->img_all_flip : xbuf;
         MEM_STEP(exec_fft(P, CUFFT_C2R, P.n_images, specN, NN, spec, flip_imgs, work, s));
         MEM_STEP(kern::intensity(P, flip_imgs, pds, out->img_all_intensity, s));
     }
+    MEM_STEP(mark(8));
     // (a10) D
     if (!P.params.avg_only && out->D) {
         const Tile* tiles = at<Tile>(ws, L.tiles);
@@ -415,8 +434,38 @@ int mem_plan_execute(mem_plan* plan, const mem_inputs* in, const mem_outputs* ou
             MEM_STEP(kern::gemm_split_bf16(P, feat_a, feat_b, pair_norm, pd_max, tiles, pds,
                                            out->D, status, s));
     }
+    MEM_STEP(mark(9));
 #undef MEM_STEP
     return MEM_OK;
+}
+
+int mem_plan_set_timing(mem_plan* plan, int enable) {
+    if (!plan) return MEM_ERR_INVALID;
+    if (enable && !plan->ev[0]) {
+        for (auto& e : plan->ev) MEM_CUDA_TRY(cudaEventCreate(&e));
+    }
+    plan->timing = enable != 0;
+    return MEM_OK;
+}
+
+int mem_plan_phase_times(mem_plan* plan, float* ms_out, int max_phases) {
+    if (!plan || !ms_out || max_phases < 0) return MEM_ERR_INVALID;
+    if (!plan->timed_run) return MEM_ERR_INVALID;
+    MEM_CUDA_TRY(cudaEventSynchronize(plan->ev[MEM_NUM_PHASES]));
+    const int n = std::min(max_phases, MEM_NUM_PHASES);
+    for (int i = 0; i < n; ++i) {
+        float ms = 0.f;
+        if (plan->phase_ran[i]) MEM_CUDA_TRY(cudaEventElapsedTime(&ms, plan->ev[i], plan->ev[i + 1]));
+        ms_out[i] = ms;
+    }
+    return MEM_NUM_PHASES;
+}
+
+const char* mem_phase_name(int phase) {
+    static const char* names[MEM_NUM_PHASES] = {"gather", "lowpass", "rotate", "spectrum",
+                                                "sums", "features", "averages", "flip",
+                                                "contraction"};
+    return (phase >= 0 && phase < MEM_NUM_PHASES) ? names[phase] : "";
 }
 
 int mem_workspace_status(const mem_plan* plan, const void* workspace) {

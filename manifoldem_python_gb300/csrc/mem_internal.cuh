@@ -77,6 +77,14 @@ struct mem_plan {
     size_t cufft_work_bytes = 0;
     int device = -1;
     int num_sms = 0;
+    bool timing = false;
+    bool timed_run = false;
+    cudaEvent_t ev[MEM_NUM_PHASES + 1] = {};
+    bool phase_ran[MEM_NUM_PHASES] = {};
+    ~mem_plan() {
+        for (auto& e : ev)
+            if (e) cudaEventDestroy(e);
+    }
 };
 
 namespace mem {

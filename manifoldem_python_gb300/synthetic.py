@@ -31,7 +31,7 @@ from typing import List, Optional, Sequence
 
 import numpy as np
 
-__all__ = ["SynthConfig", "Dataset", "CONFIGS", "make_dataset", "quat_from_euler",
+__all__ = ["SynthConfig", "Dataset", "CONFIGS", "make_dataset", "particle_counts", "quat_from_euler",
            "augment_quat"]
 
 
@@ -177,8 +177,15 @@ def _orientations_for(d: np.ndarray, n: int, jitter_deg: float, rng) -> np.ndarr
     return quat_from_euler(phi, theta, psi)
 
 
-def make_dataset(cfg: SynthConfig, device="cpu", dtype=None, pd_limit: Optional[int] = None) -> Dataset:
-    """Build the dataset of ``cfg``; ``pd_limit`` keeps only the first PDs (for small samples)."""
+def particle_counts(cfg: SynthConfig) -> np.ndarray:
+    """Particles per PD of ``cfg`` (the first draw of its generator)."""
+    return _particle_counts(cfg, np.random.default_rng(cfg.seed))
+
+
+def make_dataset(cfg: SynthConfig, device="cpu", dtype=None, pd_limit: Optional[int] = None,
+                 pd_select: Optional[Sequence[int]] = None) -> Dataset:
+    """Build the dataset of ``cfg``.  ``pd_limit`` keeps only the first PDs; ``pd_select`` keeps
+    the listed PDs of the full workload (same geometry), rendering only their particles."""
     import torch
 
     rng = np.random.default_rng(cfg.seed)
@@ -244,6 +251,23 @@ def make_dataset(cfg: SynthConfig, device="cpu", dtype=None, pd_limit: Optional[
     moves *= (0.15 * N) / np.linalg.norm(moves, axis=0)
     noise_seed = int(rng.integers(0, 2**62))
 
+    if pd_select is not None:
+        sel = [int(i) for i in pd_select]
+        phys = [np.where(CG[i] >= num_part, CG[i] - num_part, CG[i]) for i in sel]
+        keep = np.unique(np.concatenate(phys))
+        remap = np.full(num_part, -1, dtype=np.int64)
+        remap[keep] = np.arange(keep.size)
+        new_cg = []
+        for i, ph in zip(sel, phys):
+            conj = CG[i] >= num_part
+            new_cg.append(remap[ph] + np.where(conj, keep.size, 0))
+        CG = new_cg
+        q_orig, df_orig, latent = q_orig[:, keep], df_orig[keep], latent[keep]
+        nd = near_dup_of[keep]
+        near_dup_of = np.where(nd >= 0, remap[np.maximum(nd, 0)], -1)
+        near_dup_of[near_dup_of < 0] = -1
+        num_part = keep.size
+
     q_aug = augment_quat(q_orig)
     df_aug = np.concatenate((df_orig, df_orig))
 
@@ -274,7 +298,7 @@ def _render(cfg, q, df, latent, near_dup_of, radii, centre, amp, moves, noise_se
     g.manual_seed(noise_seed)
     radii_t = torch.as_tensor(radii, dtype=cdt, device=dev)
     amp_t = torch.as_tensor(amp, dtype=cdt, device=dev)
-    clean = []
+    s1 = s2 = 0.0
     for s in range(0, num_part, chunk):
         e = min(num_part, s + chunk)
         c = np.repeat(centre[:, :, None], e - s, axis=2)          # 3 x B x P
@@ -291,10 +315,11 @@ def _render(cfg, q, df, latent, near_dup_of, radii, centre, amp, moves, noise_se
         w = (0.5 * math.pi * cfg.cs * 1e7 * lam ** 3 * k2[None] - math.pi * lam * dfb[:, None, None]) * k2[None]
         ctf = (torch.sin(w) - cfg.ampc * torch.cos(w)) * env[None]
         img = torch.fft.ifft2(torch.fft.fft2(img) * ctf).real
-        clean.append(img)
+        s1 += float(img.sum(dtype=torch.float64))
+        s2 += float((img.to(torch.float64) ** 2).sum())
         out[s:e] = img.to(torch.float32)
-    sig_var = float(torch.cat([c.reshape(-1) for c in clean]).var()) if num_part * N * N < 2**28 \
-        else float(torch.stack([c.var() for c in clean]).mean())
+    cnt = float(num_part) * N * N
+    sig_var = max(s2 / cnt - (s1 / cnt) ** 2, 1e-30)
     sigma = math.sqrt(sig_var / cfg.snr)
     for s in range(0, num_part, chunk):
         e = min(num_part, s + chunk)
