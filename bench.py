@@ -228,9 +228,19 @@ def run_gpu(args, rank, world):
     dfd = torch.from_numpy(df_h).to(dev)
     stack = ds.stack
     stream = torch.cuda.current_stream(dev)
+    graph = None
+    if args.graph:
+        try:
+            graph = plan.capture(stack, sidx, flip, psi, dfd, outs)
+        except Exception as exc:           # report, and time direct launches instead
+            print('graph capture failed: %s' % exc, file=sys.stderr)
+            graph = None
 
     def step():
-        plan.execute(stack, sidx, flip, psi, dfd, outs, stream)
+        if graph is not None:
+            graph.replay()
+        else:
+            plan.execute(stack, sidx, flip, psi, dfd, outs, stream)
 
     for _ in range(args.warmup):
         step()
@@ -257,7 +267,7 @@ def run_gpu(args, rank, world):
     import ctypes
     lib = plan.lib
     lib.mem_plan_set_timing(plan.handle, 1)
-    step()
+    plan.execute(stack, sidx, flip, psi, dfd, outs, stream)
     phase_ms = (ctypes.c_float * 9)()
     lib.mem_plan_phase_times(plan.handle, phase_ms, 9)
     lib.mem_plan_set_timing(plan.handle, 0)
@@ -303,6 +313,7 @@ def run_gpu(args, rank, world):
         e2e = dict(ms=e2e_ms, h2d=int(h2d), d2h=int(d2h), pinned=pin)
         del stack_h, res_h
     return dict(ms=ms, pairs=plan.n_pairs, n_images=plan.n_images, counts=counts,
+                graph=graph is not None,
                 phases=phases, clocks=clk.summary(), t_gen=t_gen, e2e=e2e, ds=ds, cfg=cfg,
                 kernels=kernels_per_execute(outputs, False), outputs=outputs)
 
@@ -367,6 +378,8 @@ def main():
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--cpu-max-n', type=int, default=900)
+    ap.add_argument('--no-graph', dest='graph', action='store_false',
+                    help='launch the stage directly instead of replaying a captured CUDA graph')
     args = ap.parse_args()
 
     world = int(os.environ.get('WORLD_SIZE', '1'))
@@ -443,7 +456,8 @@ def main():
                     precision=args.precision, outputs=list(r['outputs']),
                     l2='inputs larger than L2 (%.1f GB image stack)' % (
                         r['ds'].stack.numel() * 4 / 1e9),
-                    parallelism='PD-sharded, one process per GPU' if world > 1 else 'single GPU'),
+                    parallelism='PD-sharded, one process per GPU' if world > 1 else 'single GPU',
+                    cuda_graph=r['graph']),
         roofline=dict(bound=rl['bound'], achieved=rl['achieved'], peak=rl['peak'],
                       unit=rl['unit'], frac=rl['frac'], traffic=rl['traffic'],
                       kernel=rl['phase'], peak_source=rl['peak_source']),

@@ -22,6 +22,7 @@ from .getDistanceCTF_local_Conj9combinedS2 import (OUTPUT_KEYS, assemble, read_s
                                                     stage_params)
 from .p import params_module
 from .pipeline import DEFAULT_OUTPUTS, DistanceStage, PdJob, admit_batches
+from .sharding import shard
 
 FILTER_PAR = dict(type='Butter', Qc=0.5, N=8)
 
@@ -105,6 +106,12 @@ def op(*argv):
         p.nPix = int(np.sqrt(os.path.getsize(p.img_stack_file) / (4 * p.num_part)))
         set_params.op(0)
     input_data = divide(CG, q, df, p.numberofJobs)
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    if world > 1:
+        # one process per GPU: this rank's LPT share of the pending PDs, no data exchange
+        rank = int(os.environ.get('RANK', '0'))
+        mine = shard([len(j[0]) for j in input_data], int(p.nPix), rank, world)
+        input_data = [input_data[i] for i in mine]
     progress = argv[0] if argv else None
     offset = p.numberofJobs - len(input_data)
     if progress is not None:

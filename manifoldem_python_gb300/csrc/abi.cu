@@ -2,6 +2,7 @@
 // pipeline.  See include/manifoldem_gb300.h for the contract.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -217,6 +218,9 @@ int mem_plan_create(const mem_params* params, int32_t n_pd, const int32_t* pd_co
         return MEM_ERR_UNSUPPORTED;
     }
     P->ctf = make_ctf(p, P->N);
+    // tensor-core accumulation knobs (tuning; the defaults are the validated setting)
+    if (const char* e = std::getenv("MEM_TC_GROUP_CHUNKS")) P->tc_group_chunks = std::atoi(e);
+    if (const char* e = std::getenv("MEM_TC_KAHAN")) P->tc_kahan = std::atoi(e) != 0;
 
     // cuFFT work sizes: exact when a device is current, an estimate otherwise
     std::vector<int> img_batches;

@@ -1,12 +1,413 @@
-// Split-BF16 tcgen05 form of the D contraction (placeholder until the tensor-core kernel lands).
+// Split-BF16 tcgen05 form of the all-pairs CTF distance (reference :391-397).
+//
+//   D_ij = a_i + a_j + E_ij,  E_ij = u'_i.v'_j + v'_i.u'_j - r'_i.r'_j - s'_i.s'_j
+//
+// Each feature x is stored as x_hi = bf16(x), x_lo = bf16(x - x_hi); E is accumulated as
+// A_hi.B_hi + A_hi.B_lo + A_lo.B_hi (the lo.lo term, ~2^-16 relative, is dropped) on the 5th-gen
+// tensor cores: tcgen05.mma kind::f16 (BF16 in, FP32 accumulate in TMEM), operands staged in
+// shared memory by TMA (128-byte swizzle).  B reads the same feature matrix as A with its first
+// two column blocks swapped (TMA coordinates); the r', s' blocks use the instruction
+// descriptor's negate-B bit, so one accumulator holds E.
+//
+// One CTA per upper-triangle 128 x 128 tile (pd, I, J); 10 warps:
+//   warps 0-7  epilogue: warp w reads TMEM lanes 32*(w%4).. and columns 64*(w/4)..;
+//   warp 8     TMA producer (3-stage ring of 64 KB stages: A_hi, A_lo, B_hi, B_lo, K = 64);
+//   warp 9     TMEM allocator and MMA issuer.
+// The K loop is cut into groups of `group_chunks` 64-wide chunks; each group accumulates into
+// one of two TMEM buffers and the epilogue warps add the finished group into FP32 register sums
+// (compensated), so the tensor core's FP32 accumulation only ever spans one group.
+// Every mbarrier wait is bounded: on expiry the CTA sets the status word's timeout bit, stops
+// issuing, waits (bounded) for its own TMA copies and MMAs, frees its TMEM and returns.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "mem_internal.cuh"
 
 namespace mem {
+namespace {
+
+constexpr int TC_M = 128, TC_N = 128, TC_BK = 64, TC_STAGES = 3;
+constexpr int TC_EPI_WARPS = 8;
+constexpr int TC_THREADS = (TC_EPI_WARPS + 2) * 32;
+constexpr int TC_OPB = TC_M * TC_BK * 2;          // one operand tile: 16 KB
+constexpr int TC_STAGE_BYTES = 4 * TC_OPB;        // 64 KB
+constexpr uint32_t TC_TMEM_COLS = 256;            // two 128-column FP32 accumulators
+constexpr size_t TC_SMEM = (size_t)TC_STAGES * TC_STAGE_BYTES + 1024 + 256;
+constexpr long long kWaitCycles = 4000000000ll;   // ~2 s at 2 GHz
+
+// instruction descriptor, kind::f16: D f32 (bits 4-5 = 1), A bf16 (7-9 = 1), B bf16 (10-12 = 1),
+// K-major A and B (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at bits 24-28, negate B bit 14
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TC_N >> 3) << 17) |
+                           ((uint32_t)(TC_M >> 4) << 24);
+constexpr uint32_t IDESC_NEG = IDESC | (1u << 14);
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// bounded wait; false if it expired or another role aborted
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
+                                          uint32_t* status) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity)) {
+        if (*abort_flag) return false;
+        if (clock64() - t0 > kWaitCycles) {
+            *abort_flag = 1;
+            atomicOr(status, kStatusTimeout);
+            return false;
+        }
+    }
+    return true;
+}
+
+// bounded wait used while draining after an abort (no abort check)
+__device__ __forceinline__ void mbar_drain(uint64_t* bar, uint32_t parity) {
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity))
+        if (clock64() - t0 > kWaitCycles) return;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar,
+                                            int x, int y) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+        "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart
+__device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
+    uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)1 << 16;                  // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;        // stride byte offset
+    d |= (uint64_t)1 << 46;                  // descriptor version
+    d |= (uint64_t)2 << 61;                  // SWIZZLE_128B
+    return d;
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
+                                          uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+    asm volatile(
+        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+            smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+          "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+          "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+          "=r"(r[31])
+        : "r"(taddr)
+        : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld_wait() {
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+struct TcShared {
+    uint64_t full[TC_STAGES];
+    uint64_t empty[TC_STAGES];
+    uint64_t acc_full[2];
+    uint64_t acc_empty[2];
+    uint64_t mma_done;
+    uint32_t tmem_base;
+    int abort_flag;
+};
+
+template <bool KAHAN>
+__global__ void __launch_bounds__(TC_THREADS, 1) gemm_tc_kernel(
+        const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CUtensorMap map_lo,
+        const double* __restrict__ pair_norm, const uint32_t* __restrict__ pd_max,
+        const Tile* __restrict__ tiles, const PdDev* __restrict__ pds, double* __restrict__ D,
+        uint32_t* __restrict__ status, int64_t Kc_pad, int group_chunks) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    TcShared* sh = (TcShared*)(smem + TC_STAGES * TC_STAGE_BYTES);
+    volatile int* abort_flag = &sh->abort_flag;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const Tile t = tiles[blockIdx.x];
+    const PdDev pd = pds[t.pd];
+    const int nchunks = (int)(4 * Kc_pad / TC_BK);
+    const int gsize = (group_chunks > 0 && group_chunks < nchunks) ? group_chunks : nchunks;
+    const int ngroups = (nchunks + gsize - 1) / gsize;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < TC_STAGES; ++s) {
+            mbar_init(&sh->full[s], 1);
+            mbar_init(&sh->empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&sh->acc_full[b], 1);
+            mbar_init(&sh->acc_empty[b], TC_EPI_WARPS);
+        }
+        mbar_init(&sh->mma_done, 1);
+        sh->abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == TC_EPI_WARPS + 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(&sh->tmem_base)),
+                     "r"(TC_TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = sh->tmem_base;
+    const int rowA = (int)(pd.row_off + (int64_t)t.I * TC_M);
+    const int rowB = (int)(pd.row_off + (int64_t)t.J * TC_N);
+
+    if (warp == TC_EPI_WARPS) {
+        // ---------------------------------------------------------------- TMA producer
+        if (lane == 0) {
+            asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&map_hi) : "memory");
+            asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&map_lo) : "memory");
+            int issued = 0;
+            for (int c = 0; c < nchunks; ++c) {
+                const int st = c % TC_STAGES;
+                const uint32_t ph = (uint32_t)(c / TC_STAGES) & 1u;
+                if (c >= TC_STAGES && !mbar_wait(&sh->empty[st], ph ^ 1u, abort_flag, status))
+                    break;
+                const int64_t ka = (int64_t)c * TC_BK;
+                const int64_t kb = ka < Kc_pad ? ka + Kc_pad : (ka < 2 * Kc_pad ? ka - Kc_pad : ka);
+                uint8_t* sb = smem + st * TC_STAGE_BYTES;
+                mbar_expect_tx(&sh->full[st], TC_STAGE_BYTES);
+                tma_load_2d(sb + 0 * TC_OPB, &map_hi, &sh->full[st], (int)ka, rowA);
+                tma_load_2d(sb + 1 * TC_OPB, &map_lo, &sh->full[st], (int)ka, rowA);
+                tma_load_2d(sb + 2 * TC_OPB, &map_hi, &sh->full[st], (int)kb, rowB);
+                tma_load_2d(sb + 3 * TC_OPB, &map_lo, &sh->full[st], (int)kb, rowB);
+                issued = c + 1;
+            }
+            if (*abort_flag) {   // let the copies already issued land before the CTA exits
+                for (int c = (issued > TC_STAGES ? issued - TC_STAGES : 0); c < issued; ++c)
+                    mbar_drain(&sh->full[c % TC_STAGES], (uint32_t)(c / TC_STAGES) & 1u);
+            }
+        }
+    } else if (warp == TC_EPI_WARPS + 1) {
+        // ---------------------------------------------------------------- MMA issuer
+        if (lane == 0) {
+            bool issued_any = false;
+            for (int c = 0; c < nchunks; ++c) {
+                const int st = c % TC_STAGES;
+                const uint32_t ph = (uint32_t)(c / TC_STAGES) & 1u;
+                const int g = c / gsize;
+                const int b = g & 1;
+                const bool first = (c % gsize) == 0;
+                const bool last = ((c % gsize) == gsize - 1) || c == nchunks - 1;
+                if (first && g >= 2 &&
+                    !mbar_wait(&sh->acc_empty[b], (uint32_t)((g >> 1) - 1) & 1u, abort_flag,
+                               status))
+                    break;
+                if (!mbar_wait(&sh->full[st], ph, abort_flag, status)) break;
+                tc_fence_after();
+                const uint32_t idesc = ((int64_t)c * TC_BK >= 2 * Kc_pad) ? IDESC_NEG : IDESC;
+                const uint32_t d = tmem + (uint32_t)(b * TC_N);
+                const uint32_t sa = smem_u32(smem + st * TC_STAGE_BYTES);
+#pragma unroll
+                for (int k = 0; k < TC_BK / 16; ++k) {
+                    const uint64_t ahi = sdesc_sw128(sa + 0 * TC_OPB + k * 32);
+                    const uint64_t alo = sdesc_sw128(sa + 1 * TC_OPB + k * 32);
+                    const uint64_t bhi = sdesc_sw128(sa + 2 * TC_OPB + k * 32);
+                    const uint64_t blo = sdesc_sw128(sa + 3 * TC_OPB + k * 32);
+                    umma_bf16(d, ahi, bhi, idesc, (first && k == 0) ? 0u : 1u);
+                    umma_bf16(d, ahi, blo, idesc, 1u);
+                    umma_bf16(d, alo, bhi, idesc, 1u);
+                }
+                issued_any = true;
+                umma_commit(&sh->empty[st]);
+                if (last) umma_commit(&sh->acc_full[b]);
+            }
+            if (*abort_flag && issued_any) {   // wait for the MMAs in flight
+                umma_commit(&sh->mma_done);
+                mbar_drain(&sh->mma_done, 0);
+            }
+        }
+    } else {
+        // ---------------------------------------------------------------- epilogue
+        const int q = warp & 3, h = warp >> 2;
+        const int row = q * 32 + lane;
+        float acc[64], cmp[64];
+#pragma unroll
+        for (int j = 0; j < 64; ++j) acc[j] = cmp[j] = 0.f;
+        bool ok = true;
+        for (int g = 0; g < ngroups && ok; ++g) {
+            const int b = g & 1;
+            ok = mbar_wait(&sh->acc_full[b], (uint32_t)(g >> 1) & 1u, abort_flag, status);
+            __syncwarp();
+            ok = __all_sync(0xffffffffu, ok);
+            if (!ok) break;
+            tc_fence_after();
+            const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * TC_N + h * 64);
+#pragma unroll
+            for (int half = 0; half < 2; ++half) {
+                uint32_t r[32];
+                tmem_ld32(taddr + half * 32, r);
+                tmem_ld_wait();
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    const float x = __uint_as_float(r[j]);
+                    float& s = acc[half * 32 + j];
+                    if (KAHAN) {
+                        float& c = cmp[half * 32 + j];
+                        const float y = x - c;
+                        const float tt = s + y;
+                        c = (tt - s) - y;
+                        s = tt;
+                    } else {
+                        s += x;
+                    }
+                }
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&sh->acc_empty[b]);
+        }
+        if (ok && !*abort_flag) {
+            const double sc = (double)feature_scale_from_bits(pd_max[t.pd]);
+            const double inv_sc2 = 1.0 / (sc * sc);
+            const int n = pd.n;
+            const int gi = t.I * TC_M + row;
+            double* Dp = D + pd.d_off;
+            const double* an = pair_norm + pd.img_off;
+            if (gi < n) {
+                const double ai = an[gi];
+                const int j0 = t.J * TC_N + h * 64;
+#pragma unroll
+                for (int j = 0; j < 64; ++j) {
+                    const int gj = j0 + j;
+                    if (gj >= n || gj < gi) continue;
+                    if (gj == gi) {
+                        Dp[(int64_t)gi * n + gi] = 0.0;
+                        continue;
+                    }
+                    const float e = KAHAN ? (acc[j] - cmp[j]) : acc[j];
+                    const double v = ai + an[gj] + (double)e * inv_sc2;
+                    Dp[(int64_t)gi * n + gj] = v;
+                    Dp[(int64_t)gj * n + gi] = v;
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == TC_EPI_WARPS + 1) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                     "r"(TC_TMEM_COLS)
+                     : "memory");
+    }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                             cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }
+    return fn;
+}
+
+int make_map(CUtensorMap* map, const void* base, int64_t K4, int64_t rows) {
+    auto enc = get_encode();
+    if (!enc) return MEM_ERR_CUDA;
+    cuuint64_t dims[2] = {(cuuint64_t)K4, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)(K4 * 2)};
+    cuuint32_t box[2] = {(cuuint32_t)TC_BK, (cuuint32_t)TC_M};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims,
+                     strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                     CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? MEM_OK : MEM_ERR_CUDA;
+}
+
+}  // namespace
+
 namespace kern {
 int gemm_split_bf16(const mem_plan& P, const void* feat_hi, const void* feat_lo,
                     const double* pair_norm, const uint32_t* pd_max, const Tile* tiles,
                     const PdDev* pds, double* D, uint32_t* status, cudaStream_t s) {
-    return MEM_ERR_UNSUPPORTED;
+    if (P.tiles.empty() || !D) return MEM_OK;
+    const int64_t K4 = 4 * P.Kc_pad;
+    if (K4 % TC_BK != 0 || P.n_rows % TC_M != 0) return MEM_ERR_INVALID;
+    CUtensorMap mhi, mlo;
+    int st = make_map(&mhi, feat_hi, K4, P.n_rows);
+    if (st != MEM_OK) return st;
+    st = make_map(&mlo, feat_lo, K4, P.n_rows);
+    if (st != MEM_OK) return st;
+    if (P.tc_kahan) {
+        MEM_CUDA_TRY(cudaFuncSetAttribute(gemm_tc_kernel<true>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)TC_SMEM));
+        gemm_tc_kernel<true><<<(unsigned)P.tiles.size(), TC_THREADS, TC_SMEM, s>>>(
+            mhi, mlo, pair_norm, pd_max, tiles, pds, D, status, P.Kc_pad, P.tc_group_chunks);
+    } else {
+        MEM_CUDA_TRY(cudaFuncSetAttribute(gemm_tc_kernel<false>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)TC_SMEM));
+        gemm_tc_kernel<false><<<(unsigned)P.tiles.size(), TC_THREADS, TC_SMEM, s>>>(
+            mhi, mlo, pair_norm, pd_max, tiles, pds, D, status, P.Kc_pad, P.tc_group_chunks);
+    }
+    MEM_LAUNCH_CHECK();
+    return MEM_OK;
 }
 }  // namespace kern
 }  // namespace mem

@@ -77,6 +77,8 @@ struct mem_plan {
     size_t cufft_work_bytes = 0;
     int device = -1;
     int num_sms = 0;
+    int tc_group_chunks = 2;        // 64-wide K chunks per TMEM accumulation group (0 = all)
+    bool tc_kahan = true;           // compensated register sums across groups
     bool timing = false;
     bool timed_run = false;
     cudaEvent_t ev[MEM_NUM_PHASES + 1] = {};

@@ -127,6 +127,22 @@ class Plan:
                                              ctypes.c_void_p(stream.cuda_stream)),
                    'mem_plan_execute')
 
+    def capture(self, stack, stack_index, flip, psi_rad, df, outputs: Dict[str, object]):
+        """Capture one execute (every kernel and cuFFT launch of the stage) in a CUDA graph and
+        return it; ``graph.replay()`` reruns the stage on the same buffers.  Input and output
+        tensors must stay alive and in place while the graph is used."""
+        import torch
+        side = torch.cuda.Stream(self.device)
+        side.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(side):            # one untimed run outside capture
+            self.execute(stack, stack_index, flip, psi_rad, df, outputs, side)
+        torch.cuda.current_stream(self.device).wait_stream(side)
+        torch.cuda.synchronize(self.device)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            self.execute(stack, stack_index, flip, psi_rad, df, outputs)
+        return graph
+
     def device_status(self) -> None:
         """Raise if a bounded device-side wait expired or an input index was out of range."""
         _lib.check(self.lib.mem_workspace_status(self.handle, self.workspace.data_ptr()),

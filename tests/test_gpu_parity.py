@@ -18,7 +18,7 @@ from conftest import GOLDEN_CASES, golden_micro, golden_options, golden_ref, loa
 
 pytestmark = pytest.mark.gpu
 
-PRECISIONS = ['fp32']
+PRECISIONS = ['fp32', 'bf16x3']
 TOL_IMG = 2e-5
 
 

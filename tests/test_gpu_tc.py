@@ -1,0 +1,106 @@
+"""The split-BF16 tcgen05 contraction against the FP32 form and an FP64 contraction of the same
+spectra.  Tolerance of the split form: max |D - D64| / max |D64| <= 1e-6, where D64 is the FP64
+contraction of the GPU's own half-plane spectra and exact CTFs."""
+import dataclasses
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _dataset(N, n, near_dup=0.0, conj=0.0, seed=5):
+    from manifoldem_python_gb300.synthetic import CONFIGS, make_dataset
+    cfg = dataclasses.replace(CONFIGS['config1'], N=N, n_fixed=n, near_dup_frac=near_dup,
+                              conj_pd_frac=conj, seed=seed)
+    return cfg, make_dataset(cfg, device='cpu')
+
+
+def _run(torch, cfg, ds, precision, env=None):
+    from manifoldem_python_gb300.pipeline import DistanceStage, PdJob, StageParams
+    old = {}
+    for k, v in (env or {}).items():
+        old[k] = os.environ.get(k)
+        os.environ[k] = str(v)
+    try:
+        stage = DistanceStage(StageParams(N=cfg.N, pix_size=cfg.pix, Cs=cfg.cs, EkV=cfg.kv,
+                                          AmpContrast=cfg.ampc, precision=precision))
+        ind = ds.CG[0]
+        job = PdJob(ind=ind, q=ds.q[:, ind], df=ds.df[ind])
+        return stage.run([job], ds.stack.to('cuda'), ds.nStot,
+                         outputs=('D', 'spectrum', 'pair_norm'))[0]
+    finally:
+        for k, v in old.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+
+
+def _d64(cfg, ds, res):
+    from oracle import distance_oracle as O
+    N = cfg.N
+    F = res['spectrum'][..., 0].astype(np.float64) + 1j * res['spectrum'][..., 1]
+    Q = O.create_grid(N)
+    ind = ds.CG[0]
+    C = np.stack([np.fft.ifftshift(O.ctf_cryo_frank(Q / (2 * cfg.pix), cfg.cs, d, cfg.kv,
+                                                    np.inf, cfg.ampc))[:, :N // 2 + 1]
+                  for d in ds.df[ind]])
+    D = O.distances_from_half_plane(C, F, N)
+    np.fill_diagonal(D, 0)
+    return D
+
+
+def rel(a, b):
+    return float(np.abs(a - b).max() / np.abs(b).max())
+
+
+def test_tc_single_tile(cuda_ready):
+    """One 128x128 tile (n=24, N=32): the smallest tcgen05 launch."""
+    torch = cuda_ready
+    cfg, ds = _dataset(32, 24, conj=1.0)
+    r32 = _run(torch, cfg, ds, 'fp32')
+    rtc = _run(torch, cfg, ds, 'bf16x3')
+    D64 = _d64(cfg, ds, r32)
+    e32, etc = rel(r32['D'], D64), rel(rtc['D'], D64)
+    print('single tile: fp32 %.3g  bf16x3 %.3g' % (e32, etc))
+    np.testing.assert_array_equal(rtc['D'], rtc['D'].T)
+    assert etc < 1e-6, etc
+
+
+def test_tc_multi_tile_ragged(cuda_ready):
+    """Several PDs with ragged sizes (tiles straddling n) in one call."""
+    torch = cuda_ready
+    from manifoldem_python_gb300.pipeline import DistanceStage, PdJob, StageParams
+    cfg = dataclasses.replace(__import__('manifoldem_python_gb300.synthetic', fromlist=['x'])
+                              .CONFIGS['config4'], N=48, n_pd=5, n_median=150, n_min=1,
+                              n_max=400, seed=21)
+    from manifoldem_python_gb300.synthetic import make_dataset
+    ds = make_dataset(cfg, device='cpu')
+    jobs = [PdJob(ind=ind, q=ds.q[:, ind], df=ds.df[ind]) for ind in ds.CG]
+    res = {}
+    for prec in ('fp32', 'bf16x3'):
+        st = DistanceStage(StageParams(N=cfg.N, pix_size=cfg.pix, Cs=cfg.cs, EkV=cfg.kv,
+                                       AmpContrast=cfg.ampc, precision=prec))
+        res[prec] = st.run(jobs, ds.stack.to('cuda'), ds.nStot, outputs=('D',))
+    for a, b in zip(res['fp32'], res['bf16x3']):
+        assert rel(b['D'], a['D']) < 2e-6
+
+
+@pytest.mark.parametrize('group,kahan', [(0, 0), (1, 0), (2, 0), (4, 0), (2, 1), (8, 1)])
+def test_tc_accumulation_groups(cuda_ready, group, kahan):
+    """Near-duplicate images (cancellation) at 128 px: error of each accumulation setting."""
+    torch = cuda_ready
+    cfg, ds = _dataset(128, 384, near_dup=0.05, seed=9)
+    rtc = _run(torch, cfg, ds, 'bf16x3', env={'MEM_TC_GROUP_CHUNKS': group, 'MEM_TC_KAHAN': kahan})
+    D64 = _d64(cfg, ds, rtc)
+    e = rel(rtc['D'], D64)
+    nd = np.nonzero(ds.near_dup_of >= 0)[0]
+    src = ds.near_dup_of[nd]
+    pos = {int(v): i for i, v in enumerate(ds.CG[0])}
+    pairs = [(pos[int(a)], pos[int(b)]) for a, b in zip(nd, src) if int(a) in pos and int(b) in pos]
+    elem = max(abs(rtc['D'][i, j] - D64[i, j]) / D64[i, j] for i, j in pairs) if pairs else 0.0
+    print('group=%d kahan=%d: normwise %.3g, near-duplicate elementwise %.3g' % (group, kahan, e, elem))
+    if (group, kahan) == (2, 1):      # the default setting
+        assert e < 1e-6

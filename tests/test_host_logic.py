@@ -1,0 +1,69 @@
+"""Host-side logic of the driver: resume markers, job list, pickle format, HBM admission."""
+import os
+import pickle
+import tempfile
+
+import numpy as np
+
+from manifoldem_python_gb300 import GetDistancesS2 as G
+from manifoldem_python_gb300 import myio
+from manifoldem_python_gb300 import p as mp
+from manifoldem_python_gb300.pipeline import StageParams, admit_batches
+
+
+def _setup(tmp):
+    mp.init()
+    mp.user_dir, mp.proj_name = tmp, 'unit'
+    mp.create_dir()
+
+
+def test_divide_skips_finished_pds_and_keeps_reference_job_shape():
+    with tempfile.TemporaryDirectory() as tmp:
+        _setup(tmp)
+        CG = [np.array([0, 5]), np.array([1, 2, 3]), np.array([4])]
+        q = np.arange(4 * 6, dtype=float).reshape(4, 6)
+        df = np.arange(6, dtype=float) * 100
+        open(os.path.join(mp.dist_prog, '1'), 'a').close()        # PD 1 finished
+        open(os.path.join(mp.dist_prog, '.hidden'), 'a').close()  # ignored
+        jobs = G.divide(CG, q, df, 3)
+        assert [j[4] for j in jobs] == [0, 2]
+        ind, q1, df1, out, prD = jobs[0]
+        np.testing.assert_array_equal(q1, q[:, [0, 5]])
+        np.testing.assert_array_equal(df1, df[[0, 5]])
+        assert out == '{}prD_{}'.format(mp.dist_file, 0)
+        assert G.fileCheck() == [1] and G.count(3) == 2
+
+
+def test_myio_format_and_corrupt_file():
+    with tempfile.TemporaryDirectory() as tmp:
+        f = os.path.join(tmp, 'x')
+        myio.fout1(f, ['a', 'b'], [1, np.zeros(3)])
+        with open(f, 'rb') as fh:
+            d = pickle.load(fh)
+        assert set(d) == {'a', 'b'}
+        with open(f, 'wb') as fh:
+            fh.write(b'not a pickle')
+        assert myio.fin1(f) is None
+
+
+def test_admission_splits_by_budget_in_order():
+    params = StageParams(N=128, pix_size=2.0, Cs=2.7, EkV=300.0, AmpContrast=0.1)
+    counts = [400] * 10 + [3000]
+    b = admit_batches(counts, params, budget_bytes=int(1e9))
+    assert [i for bb in b for i in bb] == list(range(len(counts)))
+    assert len(b) > 1 and b[-1] == [10]
+    assert admit_batches(counts, params, budget_bytes=int(1e15)) == [list(range(11))]
+
+
+def test_params_module_prefers_loaded_reference_p():
+    import sys
+    import types
+    from manifoldem_python_gb300.p import params_module
+    fake = types.ModuleType('p')
+    fake.nPix = 64
+    sys.modules['p'] = fake
+    try:
+        assert params_module() is fake
+    finally:
+        del sys.modules['p']
+    assert params_module() is mp
