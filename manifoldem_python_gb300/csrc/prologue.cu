@@ -182,9 +182,9 @@ __device__ void prefilter_axis(float* s, int N, int P, int axis, int nseg, float
     // causal start value c+[k0] = sum_j z1^j s[k0 - j]
     if (active && k0 <= k1) {
         float acc = 0.f, zp = 1.f;
-        for (int j = 0; j < taps; ++j) {
+        for (int j = 0; j < taps; ++j) {      // taps <= N: one wrap at most
             int idx = k0 - j;
-            idx += (idx < 0) ? N * ((-idx + N - 1) / N) : 0;
+            idx += (idx < 0) ? N : 0;
             acc += zp * base[idx * stride_k];
             zp *= kZ1;
         }
@@ -205,7 +205,7 @@ __device__ void prefilter_axis(float* s, int N, int P, int axis, int nseg, float
         float acc = 0.f, zp = 1.f;
         for (int j = 0; j < taps; ++j) {
             int idx = k1 + j;
-            idx -= (idx >= N) ? N * (idx / N) : 0;
+            idx -= (idx >= N) ? N : 0;
             acc += zp * base[idx * stride_k];
             zp *= kZ1;
         }
@@ -233,31 +233,44 @@ __device__ __forceinline__ void bspline_w(float t, float w[4]) {
     w[2] = (2.0f / 3.0f) - u2 * (1.0f - 0.5f * u);
 }
 
-__device__ __forceinline__ float sample_bspline(const float* s, int N, int P, const RotConst& R,
-                                                int r, int c) {
-    const int64_t X = R.bx + (int64_t)r * R.rc + (int64_t)c * R.rs;
-    const int64_t Y = R.by - (int64_t)r * R.rs + (int64_t)c * R.rc;
+// wrapped index of i in [-N, 2N)
+__device__ __forceinline__ int wrapN(int i, int N) {
+    i += (i < 0) ? N : 0;
+    return i - ((i >= N) ? N : 0);
+}
+
+// one output sample at fixed-point coordinates (X, Y) (32 fractional bits)
+__device__ __forceinline__ float sample_at(const float* s, int N, int P, int64_t X, int64_t Y) {
     const int ix = (int)(X >> 32), iy = (int)(Y >> 32);
     const float tx = (float)(uint32_t)(X & 0xffffffffll) * 2.3283064365386963e-10f;
     const float ty = (float)(uint32_t)(Y & 0xffffffffll) * 2.3283064365386963e-10f;
     float wx[4], wy[4];
     bspline_w(tx, wx);
     bspline_w(ty, wy);
-    int cols[4];
+    const int r0 = wrapN(ix - 1, N), c0 = wrapN(iy - 1, N);
+    int rows[4], cols[4];
+    rows[0] = r0 * P;
+    cols[0] = c0;
 #pragma unroll
-    for (int j = 0; j < 4; ++j) cols[j] = (iy - 1 + j + 2 * N) % N;
+    for (int j = 1; j < 4; ++j) {
+        const int rj = r0 + j, cj = c0 + j;
+        rows[j] = (rj >= N ? rj - N : rj) * P;
+        cols[j] = cj >= N ? cj - N : cj;
+    }
     float acc = 0.f;
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-        const float* row = s + ((ix - 1 + i + 2 * N) % N) * P;
+        const float* row = s + rows[i];
         const float v = wy[0] * row[cols[0]] + wy[1] * row[cols[1]] + wy[2] * row[cols[2]] +
                         wy[3] * row[cols[3]];
-        acc += wx[i] * v;
+        acc = fmaf(wx[i], v, acc);
     }
     return acc;
 }
 
-template <int NT>
+// Thread t owns column c = t % N and rows r = t / N + k R (R = NT / N rows per pass), so its
+// sample coordinates advance by a constant fixed-point step.
+template <int NT, int MAXV>
 __global__ void __launch_bounds__(NT) rotate_kernel(
         float* __restrict__ xbuf, float* __restrict__ img_out, const double* __restrict__ psi_rad,
         const PdDev* __restrict__ pds, const int32_t* __restrict__ img_pd, int N, int P,
@@ -267,6 +280,10 @@ __global__ void __launch_bounds__(NT) rotate_kernel(
     const int64_t img = blockIdx.x;
     const int NN = N * N;
     float* xi = xbuf + img * (int64_t)NN;
+    const int R = NT / N;                       // rows per pass
+    const int c = threadIdx.x % N;
+    const int r0 = threadIdx.x / N;
+    const bool active = r0 < R;
     if (threadIdx.x == 0) {
         // first rotation: rotatefill(img, -(180/pi) Psi) -> t = deg2rad(that)
         const double ang = -(180.0 / 3.141592653589793) * psi_rad[img];
@@ -283,25 +300,47 @@ __global__ void __launch_bounds__(NT) rotate_kernel(
     __syncthreads();
     prefilter_axis<NT>(s, N, P, 0, nseg, inv1mzN, exact_init != 0);
     prefilter_axis<NT>(s, N, P, 1, nseg, inv1mzN, exact_init != 0);
-    const RotConst R1 = rot[0];
-    for (int p = threadIdx.x; p < NN; p += NT) {
-        const int r = p / N, c = p - r * N;
-        xi[p] = sample_bspline(s, N, P, R1, r, c);
+    float keep[MAXV > 0 ? MAXV : 1];
+    {
+        const RotConst Q = rot[0];
+        int64_t X = Q.bx + (int64_t)r0 * Q.rc + (int64_t)c * Q.rs;
+        int64_t Y = Q.by - (int64_t)r0 * Q.rs + (int64_t)c * Q.rc;
+        const int64_t dX = (int64_t)R * Q.rc, dY = -(int64_t)R * Q.rs;
+        if (MAXV > 0) {
+#pragma unroll
+            for (int k = 0; k < MAXV; ++k) {
+                const int r = r0 + k * R;
+                if (active && r < N) keep[k] = sample_at(s, N, P, X, Y);
+                X += dX;
+                Y += dY;
+            }
+        } else if (active) {
+            for (int r = r0; r < N; r += R, X += dX, Y += dY) xi[r * N + c] = sample_at(s, N, P, X, Y);
+        }
     }
     __syncthreads();
-    for (int p = threadIdx.x; p < NN; p += NT) {
-        const int r = p / N, c = p - r * N;
-        s[r * P + c] = xi[p];
+    if (MAXV > 0) {
+#pragma unroll
+        for (int k = 0; k < MAXV; ++k) {
+            const int r = r0 + k * R;
+            if (active && r < N) s[r * P + c] = keep[k];
+        }
+    } else {
+        for (int p = threadIdx.x; p < NN; p += NT) {
+            const int r = p / N, cc = p - r * N;
+            s[r * P + cc] = xi[p];
+        }
     }
     __syncthreads();
     prefilter_axis<NT>(s, N, P, 0, nseg, inv1mzN, exact_init != 0);
     prefilter_axis<NT>(s, N, P, 1, nseg, inv1mzN, exact_init != 0);
-    const RotConst R2 = rot[1];
+    if (!active) return;
+    const RotConst Q = rot[1];
+    int64_t X = Q.bx + (int64_t)r0 * Q.rc + (int64_t)c * Q.rs;
+    int64_t Y = Q.by - (int64_t)r0 * Q.rs + (int64_t)c * Q.rc;
+    const int64_t dX = (int64_t)R * Q.rc, dY = -(int64_t)R * Q.rs;
     float* out = img_out + img * (int64_t)NN;
-    for (int p = threadIdx.x; p < NN; p += NT) {
-        const int r = p / N, c = p - r * N;
-        out[p] = sample_bspline(s, N, P, R2, r, c);
-    }
+    for (int r = r0; r < N; r += R, X += dX, Y += dY) out[r * N + c] = sample_at(s, N, P, X, Y);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -565,10 +604,19 @@ int rotate(const mem_plan& P, const mem_inputs& in, float* xbuf, float* img_out,
     const bool exact = N < kInitTaps;
     if (exact) nseg = 1;
     const float inv1mzN = (float)(1.0 / (1.0 - std::pow((double)kZ1, (double)N)));
-    MEM_CUDA_TRY(cudaFuncSetAttribute(rotate_kernel<NT>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    rotate_kernel<NT><<<(unsigned)P.n_images, NT, smem, s>>>(
-        xbuf, img_out, in.psi_rad, pd_table, img_pd, N, Pst, nseg, inv1mzN, exact ? 1 : 0);
+    const int R = NT / N;
+    const int per_thread = (N + R - 1) / R;
+    if (per_thread <= 32) {
+        MEM_CUDA_TRY(cudaFuncSetAttribute(rotate_kernel<NT, 32>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        rotate_kernel<NT, 32><<<(unsigned)P.n_images, NT, smem, s>>>(
+            xbuf, img_out, in.psi_rad, pd_table, img_pd, N, Pst, nseg, inv1mzN, exact ? 1 : 0);
+    } else {
+        MEM_CUDA_TRY(cudaFuncSetAttribute(rotate_kernel<NT, 0>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        rotate_kernel<NT, 0><<<(unsigned)P.n_images, NT, smem, s>>>(
+            xbuf, img_out, in.psi_rad, pd_table, img_pd, N, Pst, nseg, inv1mzN, exact ? 1 : 0);
+    }
     MEM_LAUNCH_CHECK();
     return MEM_OK;
 }
