@@ -44,6 +44,15 @@ def load_reference():
     return ref_p, ref_op
 
 
+def reference_dm(D, seed=0):
+    """The reference's diffusion-map embedding of D (k = nS, tune 3, as the manifold stage calls
+    it, manifoldTrimmingAuto.py:51-54), with np.random seeded first."""
+    import DMembeddingII                                # noqa: E402
+    np.random.seed(seed)
+    lamb, psi, sigma = DMembeddingII.op(np.array(D, copy=True), D.shape[0], 3, 60000)[:3]
+    return lamb, psi, sigma
+
+
 # name -> (synthetic config overrides, microscope overrides, options overrides,
 #          image indices kept of the (nS, N, N) outputs; None keeps them whole)
 CASES = {
@@ -114,6 +123,9 @@ def make_case(name):
             rec['ref_' + k] = np.asarray(res[k])
     if slice_idx is not None:
         rec['slice_idx'] = np.array(slice_idx)
+    if not options['avgOnly'] and ind.shape[0] >= 40:
+        lamb, psi, sigma = reference_dm(res['D'])
+        rec.update(ref_dm_lambda=lamb, ref_dm_psi8=psi[:, :8], ref_dm_sigma=sigma)
     path = os.path.join(HERE, name + '.npz')
     np.savez_compressed(path, **rec)
     print('wrote', path, os.path.getsize(path) // 1024, 'KiB')

@@ -77,6 +77,15 @@ def test_stage_matches_reference(cuda_ready, case, precision):
     tol = 1e-6 if precision == 'bf16x3' else 2e-6
     assert rel(D, D64) < tol, (case, rel(D, D64))
     assert n == D.shape[0]
+    if 'ref_dm_psi8' in g:
+        # downstream: top-8 diffusion-map coordinates of the GPU D vs the reference's
+        from scipy.linalg import subspace_angles
+        from oracle.dm_embedding import dm_embedding
+        _, psi, _ = dm_embedding(D, seed=0)
+        ang = float(np.max(subspace_angles(psi[:, :8], g['ref_dm_psi8'])))
+        print('%s %s: D rel %.3g (vs FP64 contraction %.3g), DM top-8 angle %.3g rad'
+              % (case, precision, rel(D, Dref), rel(D, D64), ang))
+        assert ang < 1e-4, ang
 
 
 def test_batched_equals_single(cuda_ready):

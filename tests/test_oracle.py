@@ -103,3 +103,15 @@ def test_centred_decomposition_is_exact():
     D = a[:, None] + a[None, :] + E
     Dref = O.distances_from_half_plane(C, F, N)
     assert np.abs(D - Dref).max() / np.abs(Dref).max() < 1e-12
+
+
+@pytest.mark.parametrize('case', ['config1', 'even48_neardup'])
+def test_dm_embedding_matches_reference(case):
+    """The diffusion-map restatement against the reference's DMembeddingII on the reference D."""
+    from scipy.linalg import subspace_angles
+    from oracle.dm_embedding import dm_embedding
+    g = load_golden(case)
+    lam, psi, sigma = dm_embedding(g['ref_D'], seed=0)
+    assert abs(sigma - float(g['ref_dm_sigma'])) / sigma < 1e-8
+    assert np.abs(lam - g['ref_dm_lambda']).max() < 1e-9
+    assert np.max(subspace_angles(psi[:, :8], g['ref_dm_psi8'])) < 1e-8
