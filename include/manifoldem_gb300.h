@@ -44,6 +44,8 @@ extern "C" {
 #define MEM_ERR_CUFFT            -5  /* a cuFFT call failed                                      */
 #define MEM_ERR_DEVICE_TIMEOUT   -6  /* a bounded device-side wait expired (kernel returned)     */
 #define MEM_ERR_NO_DEVICE        -7  /* no sm_103 device is current                              */
+#define MEM_ERR_TOO_LARGE        -8  /* problem larger than the static scratch of the no-allocation
+                                        entry point (MEM_NOALLOC_SCRATCH_BYTES)                    */
 
 /* contraction forms for D */
 #define MEM_PREC_FP32        0   /* plain FP32 SIMT contraction, FP64 epilogue                   */
@@ -147,6 +149,29 @@ const char* mem_phase_name(int phase);
 int mem_pd_batch(const mem_params* params, int32_t n_pd, const int32_t* pd_count,
                  const double* psi_p_deg, const mem_inputs* in, const mem_outputs* out,
                  void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---- no-allocation entry point ---------------------------------------------------------
+ * No counterpart in the reference (which has no GPU path).  For callers that cannot allocate
+ * device memory at all -- a plugin running inside a host application that owns every device
+ * buffer and grants no allocation rights, code called back from another runtime's memory pool,
+ * or a latency-critical path that must not pay for cudaMalloc or fragment the heap -- this
+ * computes D for ONE PD from the PD's half-plane spectra (the mem_outputs.spectrum layout,
+ * fft2(imgAll) as (re, im) float pairs, [n][N][N/2+1]) and defocus values, with every
+ * intermediate in a file-scope static device array of MEM_NOALLOC_SCRATCH_BYTES.  It calls no
+ * cudaMalloc, cudaFree or allocating library routine (no cuFFT).
+ *   - spectra, df (device, [n]) and D (device, n*n doubles, row-major) are the caller's;
+ *     params->avg_only is ignored; params->precision selects the contraction form.
+ *   - The first call on a device resolves the array's device address on that device (make it
+ *     current first); make that first call before any stream capture.
+ *   - Sizes whose scratch (feature matrix rows padded to 128, spectra copy, sums) would exceed
+ *     MEM_NOALLOC_SCRATCH_BYTES return MEM_ERR_TOO_LARGE without launching anything; at 128 px
+ *     that allows n <= 128 images, at 70 px n <= 512; boxes above 177 px do not fit.
+ *   - Every call on a device shares the one array and it keeps the last call's contents (the
+ *     call re-initialises what it needs); calls that overlap on the GPU (other streams, other
+ *     host threads) race on it and must be serialised by the caller.                          */
+#define MEM_NOALLOC_SCRATCH_BYTES (32u << 20)
+int mem_pd_distances_noalloc(const mem_params* params, int32_t n, const float* spectra,
+                             const double* df, double* D, void* stream);
 
 #ifdef __cplusplus
 }

@@ -20,7 +20,7 @@ REPO = os.path.dirname(HERE)
 INCLUDE = os.path.join(REPO, 'include')
 BUILD_DIR = os.path.join(REPO, '_build')
 LIB_PATH = os.path.join(HERE, 'libmanifoldem_gb300.so')
-SOURCES = ['abi.cu', 'prologue.cu', 'gemm_fp32.cu', 'gemm_tc.cu']
+SOURCES = ['abi.cu', 'prologue.cu', 'gemm_fp32.cu', 'gemm_tc.cu', 'noalloc.cu']
 ARCH_FLAGS = ['-gencode', 'arch=compute_103a,code=sm_103a']
 
 # status codes (include/manifoldem_gb300.h)
@@ -32,6 +32,7 @@ MEM_ERR_CUDA = -4
 MEM_ERR_CUFFT = -5
 MEM_ERR_DEVICE_TIMEOUT = -6
 MEM_ERR_NO_DEVICE = -7
+MEM_ERR_TOO_LARGE = -8
 MEM_PREC_FP32 = 0
 MEM_PREC_SPLIT_BF16 = 1
 MEM_FILTER_BUTTER = 0
@@ -139,6 +140,8 @@ SIGNATURES = {
     'mem_plan_set_timing': (c_int32, [c_void_p, c_int32]),
     'mem_plan_phase_times': (c_int32, [c_void_p, ctypes.POINTER(ctypes.c_float), c_int32]),
     'mem_phase_name': (ctypes.c_char_p, [c_int32]),
+    'mem_pd_distances_noalloc': (c_int32, [ctypes.POINTER(MemParams), c_int32, c_void_p,
+                                            c_void_p, c_void_p, c_void_p]),
     'mem_pd_batch': (c_int32, [ctypes.POINTER(MemParams), c_int32, c_void_p, c_void_p,
                                ctypes.POINTER(MemInputs), ctypes.POINTER(MemOutputs), c_void_p,
                                c_size_t, c_void_p]),

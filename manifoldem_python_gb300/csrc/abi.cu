@@ -153,6 +153,7 @@ const char* mem_status_string(int status) {
         case MEM_ERR_CUFFT: return "cuFFT error";
         case MEM_ERR_DEVICE_TIMEOUT: return "bounded device-side wait expired";
         case MEM_ERR_NO_DEVICE: return "no CUDA device";
+        case MEM_ERR_TOO_LARGE: return "too large for the no-allocation entry point's static scratch";
         default: return "unknown status";
     }
 }
