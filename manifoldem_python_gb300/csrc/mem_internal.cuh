@@ -10,7 +10,7 @@
 
 namespace mem {
 
-constexpr int kMaxN = 236;          // rotation kernel keeps one N x (N|1) float image in smem
+constexpr int kMaxN = 236;          // rotation kernel keeps one (N+3) x (N+3)|1 float image in smem
 constexpr int kRowBlock = 128;      // PD rows are padded to this in the feature matrix
 constexpr int kKPad = 64;           // each feature block is padded to a multiple of this
 constexpr int kSumChunk = 256;      // images per partial-sum item of the per-PD reductions

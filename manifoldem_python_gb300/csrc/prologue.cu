@@ -18,7 +18,7 @@ namespace mem {
 namespace {
 
 constexpr float kZ1 = -0.26794919243112270f;     // sqrt(3) - 2, cubic B-spline pole
-constexpr int kInitTaps = 24;                      // |z1|^24 = 1.9e-14
+constexpr int kInitTaps = 18;                      // |z1|^18 = 5e-11
 
 __device__ __forceinline__ float mask_ref(int r, int c, int N) {
     // annularMask.op(0, N/2, N, N) (annularMask.py:19-32): centre (N/2 - 1, N/2), radius N/2
@@ -239,6 +239,23 @@ __device__ __forceinline__ int wrapN(int i, int N) {
     return i - ((i >= N) ? N : 0);
 }
 
+// The coefficient image sits in smem with a 3-pixel periodic halo: rows/columns N..N+2 repeat
+// 0..2, so the 4x4 taps at (r0..r0+3, c0..c0+3), r0, c0 in [0, N), need no further wrapping.
+template <int NT>
+__device__ __forceinline__ void fill_halo(float* s, int N, int P) {
+    __syncthreads();
+    for (int p = threadIdx.x; p < 3 * N; p += NT) {
+        const int r = p / N, c = p - r * N;
+        s[(N + r) * P + c] = s[r * P + c];
+    }
+    __syncthreads();
+    for (int p = threadIdx.x; p < 3 * (N + 3); p += NT) {
+        const int r = p / 3, c = p - r * 3;
+        s[r * P + N + c] = s[r * P + c];
+    }
+    __syncthreads();
+}
+
 // one output sample at fixed-point coordinates (X, Y) (32 fractional bits)
 __device__ __forceinline__ float sample_at(const float* s, int N, int P, int64_t X, int64_t Y) {
     const int ix = (int)(X >> 32), iy = (int)(Y >> 32);
@@ -247,22 +264,12 @@ __device__ __forceinline__ float sample_at(const float* s, int N, int P, int64_t
     float wx[4], wy[4];
     bspline_w(tx, wx);
     bspline_w(ty, wy);
-    const int r0 = wrapN(ix - 1, N), c0 = wrapN(iy - 1, N);
-    int rows[4], cols[4];
-    rows[0] = r0 * P;
-    cols[0] = c0;
-#pragma unroll
-    for (int j = 1; j < 4; ++j) {
-        const int rj = r0 + j, cj = c0 + j;
-        rows[j] = (rj >= N ? rj - N : rj) * P;
-        cols[j] = cj >= N ? cj - N : cj;
-    }
+    const float* base = s + wrapN(ix - 1, N) * P + wrapN(iy - 1, N);
     float acc = 0.f;
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-        const float* row = s + rows[i];
-        const float v = wy[0] * row[cols[0]] + wy[1] * row[cols[1]] + wy[2] * row[cols[2]] +
-                        wy[3] * row[cols[3]];
+        const float* row = base + i * P;
+        const float v = wy[0] * row[0] + wy[1] * row[1] + wy[2] * row[2] + wy[3] * row[3];
         acc = fmaf(wx[i], v, acc);
     }
     return acc;
@@ -300,6 +307,7 @@ __global__ void __launch_bounds__(NT) rotate_kernel(
     __syncthreads();
     prefilter_axis<NT>(s, N, P, 0, nseg, inv1mzN, exact_init != 0);
     prefilter_axis<NT>(s, N, P, 1, nseg, inv1mzN, exact_init != 0);
+    fill_halo<NT>(s, N, P);
     float keep[MAXV > 0 ? MAXV : 1];
     {
         const RotConst Q = rot[0];
@@ -334,6 +342,7 @@ __global__ void __launch_bounds__(NT) rotate_kernel(
     __syncthreads();
     prefilter_axis<NT>(s, N, P, 0, nseg, inv1mzN, exact_init != 0);
     prefilter_axis<NT>(s, N, P, 1, nseg, inv1mzN, exact_init != 0);
+    fill_halo<NT>(s, N, P);
     if (!active) return;
     const RotConst Q = rot[1];
     int64_t X = Q.bx + (int64_t)r0 * Q.rc + (int64_t)c * Q.rs;
@@ -597,8 +606,8 @@ int rotate(const mem_plan& P, const mem_inputs& in, float* xbuf, float* img_out,
            const PdDev* pd_table, const int32_t* img_pd, cudaStream_t s) {
     if (P.n_images == 0) return MEM_OK;
     const int N = P.N;
-    const int Pst = (N % 2 == 0) ? N + 1 : N;
-    const size_t smem = (size_t)N * Pst * sizeof(float);
+    const int Pst = ((N + 3) % 2 == 0) ? N + 4 : N + 3;     // odd row stride, 3-px halo
+    const size_t smem = (size_t)(N + 3) * Pst * sizeof(float);
     constexpr int NT = 512;
     int nseg = std::max(1, std::min(NT / N, N / 16));
     const bool exact = N < kInitTaps;
