@@ -113,12 +113,15 @@ def _oracle_pd(args):
     return int(ind.shape[0]), time.perf_counter() - t0
 
 
-def cpu_sample_tasks(ds, pds, mic):
-    """Compact per-PD inputs (stack of the PD's images, indices remapped) for the CPU port."""
+def cpu_sample_tasks(ds, pds, mic, sizes=None):
+    """Compact per-PD inputs (stack of the PD's images, indices remapped) for the CPU port;
+    with `sizes`, sub-PDs made of the first sizes[i] images of PD pds[i]."""
     tasks = []
     stack_all = ds.stack
-    for p in pds:
+    for t, p in enumerate(pds):
         ind = np.asarray(ds.CG[p])
+        if sizes is not None:
+            ind = ind[:sizes[t]]
         conj = ind >= ds.num_part
         sidx = np.where(conj, ind - ds.num_part, ind)
         n = ind.size
@@ -142,7 +145,8 @@ def run_cpu_tasks(tasks, cores):
 
 def extrapolate_pairs_per_s(res, wall, counts, cores):
     """Fit per-PD CPU time t(n) = a n + b n^2 on the sample and predict the wall time of the
-    whole workload on `cores` workers (perfect packing); returns pairs/s."""
+    whole workload on `cores` workers (perfect packing, but never below the largest PD's own
+    time); returns pairs/s."""
     n = np.array([r[0] for r in res], dtype=np.float64)
     t = np.array([r[1] for r in res], dtype=np.float64)
     A = np.vstack([n, n * n]).T
@@ -151,7 +155,9 @@ def extrapolate_pairs_per_s(res, wall, counts, cores):
     if a == 0 and b == 0:
         a = float(np.sum(t) / np.sum(n))
     counts = np.asarray(counts, dtype=np.float64)
-    total_t = float(np.sum(a * counts + b * counts * counts)) / cores
+    t_pd = a * counts + b * counts * counts
+    # one worker per PD, as the reference's pool runs it: no PD finishes faster than alone
+    total_t = max(float(np.sum(t_pd)) / cores, float(np.max(t_pd)))
     pairs = float(np.sum(counts * (counts - 1) / 2))
     return pairs / total_t, dict(a=a, b=b, sample_pairs_per_s=float(
         np.sum(n * (n - 1) / 2) / wall))
@@ -171,11 +177,13 @@ def choose_sample(counts, cores, max_n):
 
 
 # ------------------------------------------------------------------------------- GPU side
-def kernels_per_execute(outputs, avg_only):
+def kernels_per_execute(outputs, avg_only, N):
     """Kernels of this library one mem_plan_execute launches (cuFFT kernels excluded):
-    gather_normalize, lowpass_table, lowpass_apply, rotate, qfix, pd_sums, pd_finalize,
-    features, [avg_store], [intensity], [contraction]."""
-    k = 8
+    lowpass_table and either lowpass_fused (power-of-two N <= 128) or gather_normalize +
+    lowpass_apply, then rotate, qfix, pd_sums, pd_finalize, features, [avg_store],
+    [intensity], [contraction]."""
+    fused = (N & (N - 1)) == 0 and 16 <= N <= 128 and os.environ.get('MEM_FUSED_LOWPASS', '0') != '0'
+    k = 7 if fused else 8
     if 'img_avg' in outputs or 'img_avg_flip' in outputs:
         k += 1
     if 'img_all_intensity' in outputs:
@@ -315,7 +323,7 @@ def run_gpu(args, rank, world):
     return dict(ms=ms, pairs=plan.n_pairs, n_images=plan.n_images, counts=counts,
                 graph=graph is not None,
                 phases=phases, clocks=clk.summary(), t_gen=t_gen, e2e=e2e, ds=ds, cfg=cfg,
-                kernels=kernels_per_execute(outputs, False), outputs=outputs)
+                kernels=kernels_per_execute(outputs, False, cfg.N), outputs=outputs)
 
 
 def roofline(r, args):
@@ -345,22 +353,67 @@ def roofline(r, args):
                 peak_source=peaks['src'] + ' hbm', algorithmic_bytes=b)
 
 
+def precision_report(args, ds, counts, cfg, precision):
+    """D of one sample PD (about 150 images) in the benchmarked form against (a) an FP64
+    contraction of the GPU's own spectra and exact CTFs, (b) the full FP64 CPU oracle on the
+    same images, and the largest principal angle between the top-8 diffusion-map coordinates
+    of the GPU D and of the oracle D (DMembeddingII restatement, k = n, tune 3)."""
+    import torch
+    from manifoldem_python_gb300.pipeline import DistanceStage, PdJob, StageParams
+    from oracle import distance_oracle as O
+    from oracle.dm_embedding import top8_subspace_angle
+    cnt = np.asarray(counts)
+    p = int(np.argmin(np.abs(cnt - 150)))
+    ind = np.asarray(ds.CG[p])[:150]          # a sub-PD when every PD is large
+    stage = DistanceStage(StageParams(N=cfg.N, pix_size=cfg.pix, Cs=cfg.cs, EkV=cfg.kv,
+                                      AmpContrast=cfg.ampc, precision=precision))
+    res = stage.run([PdJob(ind=ind, q=ds.q[:, ind], df=ds.df[ind])], ds.stack, ds.nStot,
+                    outputs=('D', 'spectrum'))[0]
+    N = cfg.N
+    F = res['spectrum'][..., 0].astype(np.float64) + 1j * res['spectrum'][..., 1]
+    Q = O.create_grid(N)
+    C = np.stack([np.fft.ifftshift(O.ctf_cryo_frank(Q / (2 * cfg.pix), cfg.cs, d, cfg.kv,
+                                                    np.inf, cfg.ampc))[:, :N // 2 + 1]
+                  for d in ds.df[ind]])
+    D64 = O.distances_from_half_plane(C, F, N)
+    np.fill_diagonal(D64, 0)
+    D = res['D']
+    task = cpu_sample_tasks(ds, [p], dict(N=N, pix_size=cfg.pix, Cs=cfg.cs, EkV=cfg.kv,
+                                          AmpContrast=cfg.ampc), sizes=[ind.size])[0]
+    ref = O.pd_op(task[1], task[2], task[3], task[0], task[4], N=N, pix_size=cfg.pix, Cs=cfg.cs,
+                  EkV=cfg.kv, AmpContrast=cfg.ampc)['D']
+    np.fill_diagonal(ref, 0)
+    rel = lambda a, b: float(np.abs(a - b).max() / np.abs(b).max())
+    return dict(pd=p, n=int(ind.size), form=precision,
+                max_rel_err_vs_fp64_contraction=rel(D, D64),
+                max_rel_err_vs_fp64_oracle=rel(D, ref),
+                dm_top8_subspace_angle_rad=top8_subspace_angle(D, ref))
+
+
 def cpu_baseline(args, ds, counts, cfg, steps=1, budget_s=20.0):
     cores = os.cpu_count() or 1
     mic = dict(N=cfg.N, pix_size=cfg.pix, Cs=cfg.cs, EkV=cfg.kv, AmpContrast=cfg.ampc)
     pick = choose_sample(np.asarray(counts), cores, max_n=args.cpu_max_n)
-    tasks = cpu_sample_tasks(ds, pick, mic)
+    sizes = None
+    if len(pick) < 4:
+        # few (large) PDs: time sub-PDs of the largest PD at several sizes
+        big = int(np.argmax(counts))
+        top = min(int(counts[big]), args.cpu_max_n)
+        sizes = sorted(set(int(x) for x in np.linspace(max(20, top // 6), top, min(cores, 6))))
+        pick = [big] * len(sizes)
+    tasks = cpu_sample_tasks(ds, pick, mic, sizes)
     vals, walls = [], []
     for _ in range(steps):
         res, wall = run_cpu_tasks(tasks, cores)
         v, fit = extrapolate_pairs_per_s(res, wall, counts, cores)
         vals.append(v)
         walls.append(wall)
-    sample = ('%d PDs at size quantiles (n=%s) of the %s workload, one per core, FP64 CPU port '
+    ns = sizes if sizes is not None else sorted(int(counts[p]) for p in pick)
+    what = 'sub-PDs of the largest PD' if sizes is not None else 'PDs at size quantiles'
+    sample = ('%d %s (n=%s) of the %s workload, one per core, FP64 CPU port '
               '(oracle/distance_oracle.pd_op); pairs/s extrapolated to all %d PDs with '
               't(n)=a n + b n^2 fitted on the sample (a=%.3g s, b=%.3g s); sample wall %.1f s'
-              % (len(pick), sorted(int(counts[p]) for p in pick), args.config, len(counts),
-                 fit['a'], fit['b'], walls[-1]))
+              % (len(pick), what, ns, args.config, len(counts), fit['a'], fit['b'], walls[-1]))
     return dict(value=float(np.median(vals)), unit='pairs/s', cores=cores, kind='port',
                 sample=sample), walls
 
@@ -373,10 +426,12 @@ def main():
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--config', default='config4')
     ap.add_argument('--n-pd', type=int, default=0, help='override the number of PDs')
-    ap.add_argument('--precision', default='fp32', choices=['fp32', 'bf16x3'])
+    ap.add_argument('--precision', default='bf16x3', choices=['fp32', 'bf16x3'])
     ap.add_argument('--outputs', default='D,img_avg,img_avg_flip,img_all_intensity')
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--no-e2e', action='store_true')
+    ap.add_argument('--no-precision', action='store_true',
+                    help='skip the FP64 / diffusion-map precision report of one sample PD')
     ap.add_argument('--cpu-max-n', type=int, default=900)
     ap.add_argument('--no-graph', dest='graph', action='store_false',
                     help='launch the stage directly instead of replaying a captured CUDA graph')
@@ -397,16 +452,17 @@ def main():
         counts = particle_counts(cfg)[:cfg.n_pd]
         cores = os.cpu_count() or 1
         pick = choose_sample(counts, cores, max_n=args.cpu_max_n)
-        ds = make_dataset(cfg, device='cpu', pd_select=pick)
+        sizes = None
+        if len(pick) < 4:
+            big = int(np.argmax(counts))
+            top = min(int(counts[big]), args.cpu_max_n)
+            sizes = sorted(set(int(x) for x in np.linspace(max(20, top // 6), top,
+                                                            min(cores, 6))))
+            pick = [big] * len(sizes)
+        uniq = sorted(set(pick))
+        ds = make_dataset(cfg, device='cpu', pd_select=uniq)
         mic = dict(N=cfg.N, pix_size=cfg.pix, Cs=cfg.cs, EkV=cfg.kv, AmpContrast=cfg.ampc)
-        tasks = []
-        for j, p in enumerate(pick):
-            ind = np.asarray(ds.CG[j])
-            conj = ind >= ds.num_part
-            sidx = np.where(conj, ind - ds.num_part, ind)
-            n = ind.size
-            tasks.append((ds.stack[sidx].numpy(), np.arange(n) + np.where(conj, n, 0),
-                          ds.q[:, ind], ds.df[ind], 2 * n, mic))
+        tasks = cpu_sample_tasks(ds, [uniq.index(p) for p in pick], mic, sizes)
         for _ in range(args.warmup):
             run_cpu_tasks(tasks[:1], 1)
         vals, walls = [], []
@@ -416,10 +472,11 @@ def main():
             vals.append(v)
             walls.append(wall)
         v = float(np.median(vals))
-        sample = ('%d PDs at size quantiles (n=%s) of the %s workload per step, one per core, '
-                  'FP64 CPU port of the reference (oracle/); pairs/s extrapolated to all %d PDs '
-                  'by t(n)=a n + b n^2' % (len(pick), sorted(int(counts[p]) for p in pick),
-                                           args.config, len(counts)))
+        ns = sizes if sizes is not None else sorted(int(counts[p]) for p in pick)
+        sample = ('%d %s (n=%s) of the %s workload per step, one per core, FP64 CPU port of '
+                  'the reference (oracle/); pairs/s extrapolated to all %d PDs by '
+                  't(n)=a n + b n^2' % (len(pick), 'sub-PDs' if sizes else 'PDs at size quantiles',
+                                        ns, args.config, len(counts)))
         line = dict(metric=metric, value=v, unit='pairs/s', n_gpus=args.gpus, steps=args.steps,
                     warmup=args.warmup, ms_per_step=float(np.median(walls)) * 1000,
                     higher_is_better=True, scaling='weak', vs_baseline=None, dtype='f64',
@@ -448,7 +505,7 @@ def main():
     line = dict(
         metric=metric, value=value, unit='pairs/s', n_gpus=world, steps=args.steps,
         warmup=args.warmup, ms_per_step=r['ms'], higher_is_better=True, scaling='weak',
-        vs_baseline=None, dtype='f32' if args.precision == 'fp32' else 'bf16x3+f32acc',
+        vs_baseline=None, dtype={'fp32': 'f32', 'bf16x3': 'bf16x3+f32acc'}[args.precision],
         data='synthetic (seeded generator, 3-D Gaussian-blob volume, CTF, SNR %.2g)' % cfg.snr,
         config=dict(workload='%s: %d PDs, %dx%d px, n~lognormal(median %d), %d images, '
                              '%d pairs per GPU' % (args.config, len(r['counts']), cfg.N, cfg.N,
@@ -470,6 +527,8 @@ def main():
         line['e2e'] = dict(value=pairs_total / (e['ms'] * 1e-3), unit='pairs/s',
                            h2d_bytes_per_step=e['h2d'], d2h_bytes_per_step=e['d2h'],
                            ms_per_step=e['ms'], pinned=e['pinned'])
+    if not args.no_precision:
+        line['precision'] = precision_report(args, r['ds'], r['counts'], cfg, args.precision)
     if not args.no_cpu_baseline:
         cb, _ = cpu_baseline(args, r['ds'], r['counts'], cfg)
         line['cpu_baseline'] = cb

@@ -58,7 +58,8 @@ extern "C" {
 /* Microscope and stage parameters: the reference's module globals p.nPix, p.pix_size, p.Cs,
  * p.EkV, p.gaussEnv, p.AmpContrast, plus filterPar and options['avgOnly'].               */
 typedef struct mem_params {
-    int32_t N;              /* box size (p.nPix), 8 <= N <= 236                              */
+    int32_t N;              /* box size (p.nPix), 8 <= N <= 512 (above 236 px the rotation
+                               keeps its spline coefficients in global memory)                */
     int32_t filter_type;    /* MEM_FILTER_*                                                  */
     double  filter_Qc;      /* cutoff in units of Nyquist (filterPar['Qc'])                   */
     double  filter_order;   /* Butterworth order (filterPar['N'])                             */

@@ -96,6 +96,32 @@ T* at(void* ws, size_t off) {
     return reinterpret_cast<T*>(static_cast<char*>(ws) + off);
 }
 
+}  // namespace
+// feature column of each frequency slot k in [0, Kc_pad) (k >= Kc are zero padding): whole
+// 64-wide chunks of consecutive k are reordered by decreasing smallest |k|^2 in the chunk, so the
+// chunks holding the dominant low frequencies are accumulated last, while the columns inside a
+// chunk stay in natural order (coalesced feature stores).
+std::vector<int32_t> radius_descending_columns(int N, int64_t Kc, int64_t Kc_pad) {
+    const int Nh = N / 2 + 1;
+    const int64_t nch = Kc_pad / kKPad;
+    std::vector<int64_t> key(nch, INT64_MAX);
+    for (int64_t k = 0; k < Kc; ++k) {
+        const int ka = (int)(k / Nh), kb = (int)(k % Nh);
+        const int fa = std::min(ka, N - ka);
+        key[k / kKPad] = std::min<int64_t>(key[k / kKPad], (int64_t)fa * fa + (int64_t)kb * kb);
+    }
+    std::vector<int32_t> order(nch);
+    for (int64_t c = 0; c < nch; ++c) order[c] = (int32_t)c;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int32_t a, int32_t b) { return key[a] > key[b]; });
+    std::vector<int32_t> pos(nch);
+    for (int64_t r = 0; r < nch; ++r) pos[order[r]] = (int32_t)r;
+    std::vector<int32_t> col(Kc_pad);
+    for (int64_t k = 0; k < Kc_pad; ++k) col[k] = (int32_t)(pos[k / kKPad] * kKPad + k % kKPad);
+    return col;
+}
+namespace {
+
 CtfConst make_ctf(const mem_params& p, int N) {
     CtfConst c{};
     const double lam = 12.3986 / std::sqrt((2 * 511.0 + p.EkV) * p.EkV);
@@ -219,9 +245,12 @@ int mem_plan_create(const mem_params* params, int32_t n_pd, const int32_t* pd_co
         return MEM_ERR_UNSUPPORTED;
     }
     P->ctf = make_ctf(p, P->N);
+    P->colmap = radius_descending_columns(P->N, P->Kc, P->Kc_pad);
     // tensor-core accumulation knobs (tuning; the defaults are the validated setting)
     if (const char* e = std::getenv("MEM_TC_GROUP_CHUNKS")) P->tc_group_chunks = std::atoi(e);
     if (const char* e = std::getenv("MEM_TC_KAHAN")) P->tc_kahan = std::atoi(e) != 0;
+    if (const char* e = std::getenv("MEM_TC_TERMS")) P->tc_lolo = std::atoi(e) >= 4;
+    if (const char* e = std::getenv("MEM_FUSED_LOWPASS")) P->fused_lowpass = std::atoi(e) != 0;
 
     // cuFFT work sizes: exact when a device is current, an estimate otherwise
     std::vector<int> img_batches;
@@ -270,6 +299,8 @@ int mem_plan_create(const mem_params* params, int32_t n_pd, const int32_t* pd_co
     L.qfix = take(sizeof(uint64_t) * P->n_images);
     L.gtab = take(sizeof(float) * P->N * P->Nh);
     L.pd_max = take(sizeof(uint32_t) * n_pd);
+    L.colmap = take(sizeof(int32_t) * P->Kc_pad);
+    L.twid = take(sizeof(float) * 2 * (P->N / 2 + 1));
     L.xbuf = take(sizeof(float) * NN * P->n_images);
     L.spec = take(sizeof(float) * 2 * P->Kc * P->n_images);
     L.feat_a = take(feat_elem * 4 * P->Kc_pad * P->n_rows);
@@ -325,6 +356,17 @@ int mem_plan_upload(mem_plan* plan, void* workspace, size_t workspace_bytes, voi
                                  sizeof(int32_t) * P.n_images, cudaMemcpyHostToDevice, s));
     MEM_CUDA_TRY(cudaMemcpyAsync(at<char>(workspace, L.tiles), P.tiles.data(),
                                  sizeof(Tile) * P.tiles.size(), cudaMemcpyHostToDevice, s));
+    MEM_CUDA_TRY(cudaMemcpyAsync(at<char>(workspace, L.colmap), P.colmap.data(),
+                                 sizeof(int32_t) * P.Kc_pad, cudaMemcpyHostToDevice, s));
+    // FFT twiddles exp(-2 pi i k / N), k = 0..N/2, computed in double
+    std::vector<float> tw(2 * (P.N / 2 + 1));
+    for (int k = 0; k <= P.N / 2; ++k) {
+        const double a = -2.0 * M_PI * k / P.N;
+        tw[2 * k] = (float)std::cos(a);
+        tw[2 * k + 1] = (float)std::sin(a);
+    }
+    MEM_CUDA_TRY(cudaMemcpyAsync(at<char>(workspace, L.twid), tw.data(), sizeof(float) * tw.size(),
+                                 cudaMemcpyHostToDevice, s));
     // padding rows of the feature matrices stay zero for the whole life of the workspace
     const size_t feat_elem = (P.params.precision == MEM_PREC_FP32) ? 4 : 2;
     const size_t row_bytes = feat_elem * 4 * P.Kc_pad;
@@ -382,18 +424,28 @@ int mem_plan_execute(mem_plan* plan, const mem_inputs* in, const mem_outputs* ou
     } while (0)
 
     MEM_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(uint32_t) * 4, s));
-    // (a2) gather, conjugate flip, normalisation
-    MEM_STEP(mark(0));
-    MEM_STEP(kern::gather_normalize(P, *in, xbuf, status, s));
-    MEM_STEP(mark(1));
-    // (a3) low-pass filter: R2C, multiply by G/N^2, C2R
-    MEM_STEP(exec_fft(P, CUFFT_R2C, P.n_images, NN, specN, xbuf, spec, work, s));
-    MEM_STEP(kern::lowpass(P, spec, at<float>(ws, L.gtab), s));
-    MEM_STEP(exec_fft(P, CUFFT_C2R, P.n_images, specN, NN, spec, xbuf, work, s));
-    MEM_STEP(mark(2));
+    if (P.fused_lowpass && kern::lowpass_fused_supported(P)) {
+        // (a2, a3) gather, flip, normalisation and low-pass in one shared-memory pass
+        MEM_STEP(mark(0));
+        MEM_STEP(mark(1));
+        MEM_STEP(kern::lowpass_table(P, at<float>(ws, L.gtab), s));
+        MEM_STEP(kern::lowpass_fused(P, *in, at<float>(ws, L.gtab), at<float2>(ws, L.twid), xbuf,
+                                     status, s));
+        MEM_STEP(mark(2));
+    } else {
+        // (a2) gather, conjugate flip, normalisation
+        MEM_STEP(mark(0));
+        MEM_STEP(kern::gather_normalize(P, *in, xbuf, status, s));
+        MEM_STEP(mark(1));
+        // (a3) low-pass filter: R2C, multiply by G/N^2, C2R
+        MEM_STEP(exec_fft(P, CUFFT_R2C, P.n_images, NN, specN, xbuf, spec, work, s));
+        MEM_STEP(kern::lowpass(P, spec, at<float>(ws, L.gtab), s));
+        MEM_STEP(exec_fft(P, CUFFT_C2R, P.n_images, specN, NN, spec, xbuf, work, s));
+        MEM_STEP(mark(2));
+    }
     // (a4, a6) mask and the two rotations -> imgAll
     float* img_all = out->img_all ? out->img_all : xbuf;
-    MEM_STEP(kern::rotate(P, *in, xbuf, img_all, pds, img_pd, s));
+    MEM_STEP(kern::rotate(P, *in, xbuf, img_all, pds, img_pd, spec, s));
     MEM_STEP(mark(3));
     // (a8) F = fft2(imgAll)
     MEM_STEP(exec_fft(P, CUFFT_R2C, P.n_images, NN, specN, img_all, spec, work, s));
@@ -412,8 +464,9 @@ int mem_plan_execute(mem_plan* plan, const mem_inputs* in, const mem_outputs* ou
     void* feat_a = at<char>(ws, L.feat_a);
     void* feat_b = at<char>(ws, L.feat_b);
     double* pair_norm = out->pair_norm ? out->pair_norm : at<double>(ws, L.pair_norm);
-    MEM_STEP(kern::features(P, spec, qf, pds, img_pd, img_row, means, pd_max, feat_a, feat_b,
-                            pair_norm, out->ctf, out->spectrum, s));
+    const uint32_t* scale_bits = pd_max;
+    MEM_STEP(kern::features(P, spec, qf, pds, img_pd, img_row, at<int32_t>(ws, L.colmap), means,
+                            scale_bits, feat_a, feat_b, pair_norm, out->ctf, out->spectrum, s));
     MEM_STEP(mark(6));
     // averages: one inverse transform per PD (linearity of the reference's per-image sums)
     float* avg_real = at<float>(ws, L.avg_real);
@@ -433,10 +486,10 @@ int mem_plan_execute(mem_plan* plan, const mem_inputs* in, const mem_outputs* ou
     if (!P.params.avg_only && out->D) {
         const Tile* tiles = at<Tile>(ws, L.tiles);
         if (P.params.precision == MEM_PREC_FP32)
-            MEM_STEP(kern::gemm_fp32(P, (const float*)feat_a, pair_norm, pd_max, tiles, pds,
+            MEM_STEP(kern::gemm_fp32(P, (const float*)feat_a, pair_norm, scale_bits, tiles, pds,
                                      out->D, s));
         else
-            MEM_STEP(kern::gemm_split_bf16(P, feat_a, feat_b, pair_norm, pd_max, tiles, pds,
+            MEM_STEP(kern::gemm_split_bf16(P, feat_a, feat_b, pair_norm, scale_bits, tiles, pds,
                                            out->D, status, s));
     }
     MEM_STEP(mark(9));

@@ -12,7 +12,7 @@ constexpr int TM = 128, TN = 128, BK = 16, NT = 256, APAD = 4;
 
 __global__ void __launch_bounds__(NT) gemm_fp32_kernel(
         const float* __restrict__ X, const double* __restrict__ pair_norm,
-        const uint32_t* __restrict__ pd_max, const Tile* __restrict__ tiles,
+        const uint32_t* __restrict__ scale_bits, const Tile* __restrict__ tiles,
         const PdDev* __restrict__ pds, double* __restrict__ D, int64_t Kc_pad) {
     __shared__ __align__(16) float As[2][BK][TM + APAD];
     __shared__ __align__(16) float Bs[2][BK][TN + APAD];
@@ -25,16 +25,19 @@ __global__ void __launch_bounds__(NT) gemm_fp32_kernel(
     const float* Bbase = X + (pd.row_off + (int64_t)t.J * TN) * K4;
     const int64_t nstage = K4 / BK;
 
-    auto bcol = [&](int64_t ka) -> int64_t {
-        if (ka < Kc_pad) return ka + Kc_pad;
-        if (ka < 2 * Kc_pad) return ka - Kc_pad;
-        return ka;
+    // stages interleave the four blocks (u', v', r', s') so that the dominant low-frequency
+    // columns at the end of every block are accumulated last
+    auto acol = [&](int64_t st) -> int64_t { return (st & 3) * Kc_pad + (st >> 2) * BK; };
+    auto bcol = [&](int64_t st) -> int64_t {
+        const int64_t off = (st >> 2) * BK;
+        const int blk = (int)(st & 3);
+        return blk == 0 ? Kc_pad + off : (blk == 1 ? off : blk * Kc_pad + off);
     };
 
     float4 ra[2], rb[2];
     auto gload = [&](int64_t st) {
-        const int64_t ka = st * BK;
-        const int64_t kb = bcol(ka);
+        const int64_t ka = acol(st);
+        const int64_t kb = bcol(st);
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             const int r = lrow + h * 64;
@@ -43,7 +46,7 @@ __global__ void __launch_bounds__(NT) gemm_fp32_kernel(
         }
     };
     auto sstore = [&](int buf, int64_t st) {
-        const float sg = (st * BK < 2 * Kc_pad) ? 1.0f : -1.0f;
+        const float sg = (st & 3) < 2 ? 1.0f : -1.0f;
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             const int r = lrow + h * 64;
@@ -91,7 +94,7 @@ __global__ void __launch_bounds__(NT) gemm_fp32_kernel(
     }
 
     // epilogue: D = a_i + a_j + E / scale^2 in FP64, upper triangle + mirror
-    const double sc = (double)feature_scale_from_bits(pd_max[t.pd]);
+    const double sc = (double)feature_scale_from_bits(scale_bits[t.pd]);
     const double inv_sc2 = 1.0 / (sc * sc);
     const int n = pd.n;
     double* Dp = D + pd.d_off;
@@ -120,10 +123,10 @@ __global__ void __launch_bounds__(NT) gemm_fp32_kernel(
 
 namespace kern {
 int gemm_fp32(const mem_plan& P, const float* feat, const double* pair_norm,
-              const uint32_t* pd_max, const Tile* tiles, const PdDev* pds, double* D,
+              const uint32_t* scale_bits, const Tile* tiles, const PdDev* pds, double* D,
               cudaStream_t s) {
     if (P.tiles.empty() || !D) return MEM_OK;
-    gemm_fp32_kernel<<<(unsigned)P.tiles.size(), NT, 0, s>>>(feat, pair_norm, pd_max, tiles, pds,
+    gemm_fp32_kernel<<<(unsigned)P.tiles.size(), NT, 0, s>>>(feat, pair_norm, scale_bits, tiles, pds,
                                                              D, P.Kc_pad);
     MEM_LAUNCH_CHECK();
     return MEM_OK;

@@ -167,10 +167,10 @@ struct TcShared {
     int abort_flag;
 };
 
-template <bool KAHAN>
+template <bool KAHAN, bool LOLO>
 __global__ void __launch_bounds__(TC_THREADS, 1) gemm_tc_kernel(
         const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CUtensorMap map_lo,
-        const double* __restrict__ pair_norm, const uint32_t* __restrict__ pd_max,
+        const double* __restrict__ pair_norm, const uint32_t* __restrict__ scale_bits,
         const Tile* __restrict__ tiles, const PdDev* __restrict__ pds, double* __restrict__ D,
         uint32_t* __restrict__ status, int64_t Kc_pad, int group_chunks) {
     extern __shared__ uint8_t smem_raw[];
@@ -222,8 +222,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gemm_tc_kernel(
                 const uint32_t ph = (uint32_t)(c / TC_STAGES) & 1u;
                 if (c >= TC_STAGES && !mbar_wait(&sh->empty[st], ph ^ 1u, abort_flag, status))
                     break;
-                const int64_t ka = (int64_t)c * TC_BK;
-                const int64_t kb = ka < Kc_pad ? ka + Kc_pad : (ka < 2 * Kc_pad ? ka - Kc_pad : ka);
+                // chunks interleave the four blocks (u', v', r', s') so that the dominant
+                // low-frequency columns at the end of every block are accumulated last
+                const int blk = c & 3;
+                const int64_t off = (int64_t)(c >> 2) * TC_BK;
+                const int64_t ka = blk * Kc_pad + off;
+                const int64_t kb = blk == 0 ? Kc_pad + off : (blk == 1 ? off : ka);
                 uint8_t* sb = smem + st * TC_STAGE_BYTES;
                 mbar_expect_tx(&sh->full[st], TC_STAGE_BYTES);
                 tma_load_2d(sb + 0 * TC_OPB, &map_hi, &sh->full[st], (int)ka, rowA);
@@ -254,7 +258,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gemm_tc_kernel(
                     break;
                 if (!mbar_wait(&sh->full[st], ph, abort_flag, status)) break;
                 tc_fence_after();
-                const uint32_t idesc = ((int64_t)c * TC_BK >= 2 * Kc_pad) ? IDESC_NEG : IDESC;
+                const bool neg = (c & 3) >= 2;          // r', s' blocks (see the producer)
+                const uint32_t idesc = neg ? IDESC_NEG : IDESC;
                 const uint32_t d = tmem + (uint32_t)(b * TC_N);
                 const uint32_t sa = smem_u32(smem + st * TC_STAGE_BYTES);
 #pragma unroll
@@ -266,6 +271,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gemm_tc_kernel(
                     umma_bf16(d, ahi, bhi, idesc, (first && k == 0) ? 0u : 1u);
                     umma_bf16(d, ahi, blo, idesc, 1u);
                     umma_bf16(d, alo, bhi, idesc, 1u);
+                    if (LOLO) umma_bf16(d, alo, blo, idesc, 1u);
                 }
                 issued_any = true;
                 umma_commit(&sh->empty[st]);
@@ -317,7 +323,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gemm_tc_kernel(
             if (lane == 0) mbar_arrive(&sh->acc_empty[b]);
         }
         if (ok && !*abort_flag) {
-            const double sc = (double)feature_scale_from_bits(pd_max[t.pd]);
+            const double sc = (double)feature_scale_from_bits(scale_bits[t.pd]);
             const double inv_sc2 = 1.0 / (sc * sc);
             const int n = pd.n;
             const int gi = t.I * TC_M + row;
@@ -383,7 +389,7 @@ int make_map(CUtensorMap* map, const void* base, int64_t K4, int64_t rows) {
 
 namespace kern {
 int gemm_split_bf16(const mem_plan& P, const void* feat_hi, const void* feat_lo,
-                    const double* pair_norm, const uint32_t* pd_max, const Tile* tiles,
+                    const double* pair_norm, const uint32_t* scale_bits, const Tile* tiles,
                     const PdDev* pds, double* D, uint32_t* status, cudaStream_t s) {
     if (P.tiles.empty() || !D) return MEM_OK;
     const int64_t K4 = 4 * P.Kc_pad;
@@ -393,19 +399,21 @@ int gemm_split_bf16(const mem_plan& P, const void* feat_hi, const void* feat_lo,
     if (st != MEM_OK) return st;
     st = make_map(&mlo, feat_lo, K4, P.n_rows);
     if (st != MEM_OK) return st;
+#define MEM_TC_LAUNCH(KAHAN, LOLO)                                                             \
+    do {                                                                                       \
+        MEM_CUDA_TRY(cudaFuncSetAttribute(gemm_tc_kernel<KAHAN, LOLO>,                         \
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize,         \
+                                          (int)TC_SMEM));                                      \
+        gemm_tc_kernel<KAHAN, LOLO><<<(unsigned)P.tiles.size(), TC_THREADS, TC_SMEM, s>>>(     \
+            mhi, mlo, pair_norm, scale_bits, tiles, pds, D, status, P.Kc_pad,                  \
+            P.tc_group_chunks);                                                                \
+    } while (0)
     if (P.tc_kahan) {
-        MEM_CUDA_TRY(cudaFuncSetAttribute(gemm_tc_kernel<true>,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)TC_SMEM));
-        gemm_tc_kernel<true><<<(unsigned)P.tiles.size(), TC_THREADS, TC_SMEM, s>>>(
-            mhi, mlo, pair_norm, pd_max, tiles, pds, D, status, P.Kc_pad, P.tc_group_chunks);
+        if (P.tc_lolo) MEM_TC_LAUNCH(true, true); else MEM_TC_LAUNCH(true, false);
     } else {
-        MEM_CUDA_TRY(cudaFuncSetAttribute(gemm_tc_kernel<false>,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)TC_SMEM));
-        gemm_tc_kernel<false><<<(unsigned)P.tiles.size(), TC_THREADS, TC_SMEM, s>>>(
-            mhi, mlo, pair_norm, pd_max, tiles, pds, D, status, P.Kc_pad, P.tc_group_chunks);
+        if (P.tc_lolo) MEM_TC_LAUNCH(false, true); else MEM_TC_LAUNCH(false, false);
     }
+#undef MEM_TC_LAUNCH
     MEM_LAUNCH_CHECK();
     return MEM_OK;
 }

@@ -10,7 +10,8 @@
 
 namespace mem {
 
-constexpr int kMaxN = 236;          // rotation kernel keeps one (N+3) x (N+3)|1 float image in smem
+constexpr int kMaxSmemN = 236;      // the rotation keeps one (N+3) x (N+3)|1 float image in smem
+constexpr int kMaxN = 512;          // larger boxes rotate with coefficients in global memory
 constexpr int kRowBlock = 128;      // PD rows are padded to this in the feature matrix
 constexpr int kKPad = 64;           // each feature block is padded to a multiple of this
 constexpr int kSumChunk = 256;      // images per partial-sum item of the per-PD reductions
@@ -52,7 +53,7 @@ struct CtfConst {
 
 struct Layout {
     size_t status, pd_table, sum_items, img_pd, img_row, tiles;
-    size_t item_off, qfix, gtab, pd_max;
+    size_t item_off, qfix, gtab, pd_max, colmap, twid;
     size_t xbuf, spec, feat_a, feat_b, pair_norm, partial, means, avg_spec, avg_real, cufft_work;
     size_t total;
 };
@@ -72,13 +73,17 @@ struct mem_plan {
     std::vector<mem::SumItem> items;
     std::vector<int32_t> img_pd, img_row;
     std::vector<mem::Tile> tiles;
+    std::vector<int32_t> colmap;    // feature column of frequency slot k (chunks radius-descending)
     mem::CtfConst ctf{};
     mem::Layout lay{};
     size_t cufft_work_bytes = 0;
     int device = -1;
     int num_sms = 0;
-    int tc_group_chunks = 2;        // 64-wide K chunks per TMEM accumulation group (0 = all)
-    bool tc_kahan = true;           // compensated register sums across groups
+    int tc_group_chunks = 1;        // 64-wide K chunks per TMEM accumulation group (0 = all)
+    bool tc_kahan = false;          // compensated register sums across groups
+    bool tc_lolo = false;           // add the lo.lo product (4-term split)
+    bool fused_lowpass = false;     // shared-memory FFT low-pass for power-of-two N <= 128
+                                    // (measured slower than the cuFFT path: off by default)
     bool timing = false;
     bool timed_run = false;
     cudaEvent_t ev[MEM_NUM_PHASES + 1] = {};
@@ -96,8 +101,12 @@ namespace kern {
 int gather_normalize(const mem_plan& P, const mem_inputs& in, float* xbuf, uint32_t* status,
                      cudaStream_t s);
 int lowpass(const mem_plan& P, float2* spec, float* gtab, cudaStream_t s);
+bool lowpass_fused_supported(const mem_plan& P);
+int lowpass_table(const mem_plan& P, float* gtab, cudaStream_t s);
+int lowpass_fused(const mem_plan& P, const mem_inputs& in, const float* gtab,
+                  const float2* twid, float* xbuf, uint32_t* status, cudaStream_t s);
 int rotate(const mem_plan& P, const mem_inputs& in, float* xbuf, float* img_out,
-           const PdDev* pd_table, const int32_t* img_pd, cudaStream_t s);
+           const PdDev* pd_table, const int32_t* img_pd, float2* spec, cudaStream_t s);
 int qfix(const mem_plan& P, const mem_inputs& in, uint64_t* qf, cudaStream_t s);
 int pd_sums(const mem_plan& P, const float2* spec, const uint64_t* qf, const SumItem* items,
             float* partial, cudaStream_t s);
@@ -105,9 +114,9 @@ int pd_finalize(const mem_plan& P, const float* partial, const SumItem* items,
                 const int32_t* item_off, const PdDev* pds, float* means, float2* avg_spec,
                 uint32_t* pd_max, cudaStream_t s);
 int features(const mem_plan& P, float2* spec, const uint64_t* qf, const PdDev* pds,
-             const int32_t* img_pd, const int32_t* img_row, const float* means,
-             const uint32_t* pd_max, void* feat_a, void* feat_b, double* pair_norm,
-             float* ctf_out, float* spectrum_out, cudaStream_t s);
+             const int32_t* img_pd, const int32_t* img_row, const int32_t* colmap,
+             const float* means, const uint32_t* scale_bits, void* feat_a, void* feat_b,
+             double* pair_norm, float* ctf_out, float* spectrum_out, cudaStream_t s);
 int avg_store(const mem_plan& P, const float* avg_real, double* img_avg, double* img_avg_flip,
               cudaStream_t s);
 int intensity(const mem_plan& P, const float* flip_imgs, const PdDev* pds, double* out,
@@ -115,12 +124,14 @@ int intensity(const mem_plan& P, const float* flip_imgs, const PdDev* pds, doubl
 
 // ---- D contraction (gemm_fp32.cu / gemm_tc.cu) ----------------------------------------
 int gemm_fp32(const mem_plan& P, const float* feat, const double* pair_norm,
-              const uint32_t* pd_max, const Tile* tiles, const PdDev* pds, double* D,
+              const uint32_t* scale_bits, const Tile* tiles, const PdDev* pds, double* D,
               cudaStream_t s);
 int gemm_split_bf16(const mem_plan& P, const void* feat_hi, const void* feat_lo,
-                    const double* pair_norm, const uint32_t* pd_max, const Tile* tiles,
+                    const double* pair_norm, const uint32_t* scale_bits, const Tile* tiles,
                     const PdDev* pds, double* D, uint32_t* status, cudaStream_t s);
 }  // namespace kern
+
+std::vector<int32_t> radius_descending_columns(int N, int64_t Kc, int64_t Kc_pad);
 
 // per-PD centring vectors: means[pd * means_stride + b * Kc_pad + k], blocks b = u, v, r, s
 inline int64_t means_stride(const mem_plan& P) { return 4 * P.Kc_pad; }

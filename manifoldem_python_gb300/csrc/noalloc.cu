@@ -30,7 +30,7 @@ size_t a256(size_t x) { return (x + 255) / 256 * 256; }
 
 struct NoallocLayout {
     size_t status, pd_table, items, item_off, img_pd, img_row, tiles, qfix, partial, means,
-        avg_spec, pd_max, spec, feat_a, feat_b, pair_norm, total;
+        avg_spec, pd_max, colmap, spec, feat_a, feat_b, pair_norm, total;
 };
 
 NoallocLayout layout_for(const mem_plan& P) {
@@ -54,6 +54,7 @@ NoallocLayout layout_for(const mem_plan& P) {
     L.means = take(sizeof(float) * means_stride(P));
     L.avg_spec = take(sizeof(float) * 4 * P.Kc);
     L.pd_max = take(sizeof(uint32_t));
+    L.colmap = take(sizeof(int32_t) * P.Kc_pad);
     L.spec = take(sizeof(float) * 2 * P.Kc * P.n_images);
     L.feat_a = take(feat_elem * 4 * P.Kc_pad * P.n_rows);
     L.feat_b = (feat_elem == 4) ? L.feat_a : take(feat_elem * 4 * P.Kc_pad * P.n_rows);
@@ -95,6 +96,7 @@ void one_pd_tables(mem_plan& P, const mem_params& prm, int n) {
     P.ctf.d_fix = fix(std::atan(prm.AmpContrast) / (2.0 * M_PI));
     P.ctf.q_scale = lam / (2.0 * Npix * Npix);
     P.ctf.amp = (float)std::sqrt(1.0 + prm.AmpContrast * prm.AmpContrast);
+    P.colmap = radius_descending_columns(P.N, P.Kc, P.Kc_pad);
     if (std::isinf(prm.gaussEnv) || prm.gaussEnv <= 0.0) {
         P.ctf.env_c = 0.0f;
     } else {
@@ -154,6 +156,8 @@ extern "C" int mem_pd_distances_noalloc(const mem_params* params, int32_t n, con
                                  cudaMemcpyHostToDevice, s));
     MEM_CUDA_TRY(cudaMemcpyAsync(at<char>(ws, L.tiles), P.tiles.data(),
                                  sizeof(Tile) * P.tiles.size(), cudaMemcpyHostToDevice, s));
+    MEM_CUDA_TRY(cudaMemcpyAsync(at<char>(ws, L.colmap), P.colmap.data(),
+                                 sizeof(int32_t) * P.Kc_pad, cudaMemcpyHostToDevice, s));
     // the feature kernel overwrites its spectrum with sign(C) F: work on a copy in the scratch
     MEM_CUDA_TRY(cudaMemcpyAsync(at<char>(ws, L.spec), spectra, sizeof(float) * 2 * P.Kc * n,
                                  cudaMemcpyDeviceToDevice, s));
@@ -179,6 +183,7 @@ extern "C" int mem_pd_distances_noalloc(const mem_params* params, int32_t n, con
     float2* spec = at<float2>(ws, L.spec);
     uint64_t* qf = at<uint64_t>(ws, L.qfix);
     uint32_t* pd_max = at<uint32_t>(ws, L.pd_max);
+    const uint32_t* scale_bits = pd_max;
     float* means = at<float>(ws, L.means);
     double* pair_norm = at<double>(ws, L.pair_norm);
     NA_STEP(kern::qfix(P, in, qf, s));
@@ -187,14 +192,14 @@ extern "C" int mem_pd_distances_noalloc(const mem_params* params, int32_t n, con
                               at<int32_t>(ws, L.item_off), pds, means,
                               at<float2>(ws, L.avg_spec), pd_max, s));
     NA_STEP(kern::features(P, spec, qf, pds, at<int32_t>(ws, L.img_pd), at<int32_t>(ws, L.img_row),
-                           means, pd_max, at<char>(ws, L.feat_a), at<char>(ws, L.feat_b),
-                           pair_norm, nullptr, nullptr, s));
+                           at<int32_t>(ws, L.colmap), means, scale_bits, at<char>(ws, L.feat_a),
+                           at<char>(ws, L.feat_b), pair_norm, nullptr, nullptr, s));
     if (P.params.precision == MEM_PREC_FP32)
-        NA_STEP(kern::gemm_fp32(P, at<float>(ws, L.feat_a), pair_norm, pd_max,
+        NA_STEP(kern::gemm_fp32(P, at<float>(ws, L.feat_a), pair_norm, scale_bits,
                                 at<Tile>(ws, L.tiles), pds, D, s));
     else
         NA_STEP(kern::gemm_split_bf16(P, at<char>(ws, L.feat_a), at<char>(ws, L.feat_b),
-                                      pair_norm, pd_max, at<Tile>(ws, L.tiles), pds, D,
+                                      pair_norm, scale_bits, at<Tile>(ws, L.tiles), pds, D,
                                       at<uint32_t>(ws, L.status), s));
 #undef NA_STEP
     return MEM_OK;

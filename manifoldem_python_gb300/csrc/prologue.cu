@@ -101,6 +101,60 @@ __global__ void __launch_bounds__(NT) gather_normalize_kernel(
     }
 }
 
+// float4 variant for N % 4 == 0: one 16-byte load / store per 4 pixels of a stack row; a
+// conjugate flip reverses the four lanes (the row reversal maps aligned quads to aligned quads)
+template <int NT>
+__global__ void __launch_bounds__(NT) gather_normalize_v4_kernel(
+        const float* __restrict__ stack, int64_t num_stack, const int64_t* __restrict__ sidx,
+        const uint8_t* __restrict__ flip, float* __restrict__ xbuf, int N,
+        uint32_t* __restrict__ status) {
+    __shared__ double red[32];
+    const int64_t img = blockIdx.x;
+    const int64_t s = sidx[img];
+    const int NN = N * N, NQ = NN / 4;
+    float4* dst = reinterpret_cast<float4*>(xbuf + img * (int64_t)NN);
+    if (s < 0 || s >= num_stack) {
+        if (threadIdx.x == 0) atomicOr(status, 2u);
+        const float nan = __int_as_float(0x7fc00000);
+        for (int p = threadIdx.x; p < NQ; p += NT) dst[p] = make_float4(nan, nan, nan, nan);
+        return;
+    }
+    const bool f = flip[img] != 0;
+    const float4* src = reinterpret_cast<const float4*>(stack + s * (int64_t)NN);
+    auto load = [&](int p, int& a, int& b) -> float4 {
+        const int e = 4 * p;
+        a = e / N;
+        b = e - a * N;
+        float4 v = src[(a * N + (f ? N - 4 - b : b)) >> 2];
+        if (f) v = make_float4(v.w, v.z, v.y, v.x);
+        return v;
+    };
+    KSum sum, sq;
+    for (int p = threadIdx.x; p < NQ; p += NT) {
+        int a, b;
+        const float4 v = load(p, a, b);
+        const float vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float bg = vv[j] * (1.0f - mask_ref(b + j, a, N));   // reference pixel (b+j, a)
+            sum.add(bg);
+            sq.add(bg * bg);
+        }
+    }
+    const double tot = block_sum_double<NT>((double)sum.value(), red);
+    const double tot2 = block_sum_double<NT>((double)sq.value(), red);
+    const double mean = tot / NN;
+    const double var = fmax(tot2 / NN - mean * mean, 0.0);
+    const float fmean = (float)mean;
+    const float inv = (float)(1.0 / sqrt(var));
+    for (int p = threadIdx.x; p < NQ; p += NT) {
+        int a, b;
+        const float4 v = load(p, a, b);
+        dst[p] = make_float4((v.x - fmean) * inv, (v.y - fmean) * inv, (v.z - fmean) * inv,
+                             (v.w - fmean) * inv);
+    }
+}
+
 // ------------------------------------------------------------------------------------------
 // 2. low-pass filter table G(k)/N^2 and its application (reference :139-167, :286-293)
 // ------------------------------------------------------------------------------------------
@@ -128,6 +182,216 @@ __global__ void lowpass_apply_kernel(float2* __restrict__ spec, const float* __r
         v.x *= gv;
         v.y *= gv;
         spec[e] = v;
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// 2b. fused gather + normalisation + low-pass for power-of-two N <= 128 (one CTA per image)
+//
+// Same result as gather_normalize + cuFFT R2C + lowpass_apply + cuFFT C2R, with the image kept
+// in shared memory: a real 2D FFT (rows: length-N/2 complex FFT of the packed pairs
+// (x[2j], x[2j+1]) then the real-FFT split; columns: length-N complex FFT), the multiply by
+// G/N^2, and the inverse.  Forward transforms are radix-2 decimation-in-frequency (natural in,
+// bit-reversed out), inverse transforms decimation-in-time (bit-reversed in, natural out), so
+// no reordering pass is needed; G is read at the bit-reversed row.  Twiddles
+// exp(-2 pi i k / N), k <= N/2, come from a table computed in double on the host.
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 cmulc(float2 a, float2 b) {   // a * conj(b)
+    return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+
+// radix-2 DIF over `batch` signals of length 2^logL; element (b, i) at C[b*bs + i*es]
+template <int NT>
+__device__ void fft_dif(float2* C, int logL, int batch, int bs, int es, const float2* tw, int logN,
+                        bool lanes_on_batch) {
+    const int L = 1 << logL, half = L >> 1;
+    for (int lh = logL - 1; lh >= 0; --lh) {
+        const int h = 1 << lh;
+        const int tstride = logN - lh - 1;            // twiddle index step N / (2h)
+        for (int t = threadIdx.x; t < batch * half; t += NT) {
+            int b, q;
+            if (lanes_on_batch) { b = t % batch; q = t / batch; }
+            else { b = t >> (logL - 1); q = t & (half - 1); }
+            const int j = q & (h - 1);
+            const int i0 = ((q >> lh) << (lh + 1)) + j;
+            float2* p0 = C + b * bs + i0 * es;
+            float2* p1 = p0 + h * es;
+            const float2 u = *p0, v = *p1;
+            *p0 = make_float2(u.x + v.x, u.y + v.y);
+            *p1 = cmul(make_float2(u.x - v.x, u.y - v.y), tw[j << tstride]);
+        }
+        __syncthreads();
+    }
+}
+
+// radix-2 DIT inverse (conjugate twiddles, unnormalised), bit-reversed in, natural out
+template <int NT>
+__device__ void fft_dit_inv(float2* C, int logL, int batch, int bs, int es, const float2* tw,
+                            int logN, bool lanes_on_batch) {
+    const int L = 1 << logL, half = L >> 1;
+    for (int lh = 0; lh < logL; ++lh) {
+        const int h = 1 << lh;
+        const int tstride = logN - lh - 1;
+        for (int t = threadIdx.x; t < batch * half; t += NT) {
+            int b, q;
+            if (lanes_on_batch) { b = t % batch; q = t / batch; }
+            else { b = t >> (logL - 1); q = t & (half - 1); }
+            const int j = q & (h - 1);
+            const int i0 = ((q >> lh) << (lh + 1)) + j;
+            float2* p0 = C + b * bs + i0 * es;
+            float2* p1 = p0 + h * es;
+            const float2 u = *p0;
+            const float2 v = cmulc(*p1, tw[j << tstride]);
+            *p0 = make_float2(u.x + v.x, u.y + v.y);
+            *p1 = make_float2(u.x - v.x, u.y - v.y);
+        }
+        __syncthreads();
+    }
+}
+
+__device__ __forceinline__ int bitrev(int k, int bits) { return (int)(__brev((unsigned)k) >> (32 - bits)); }
+
+template <int NT, int LOGN>
+__global__ void __launch_bounds__(NT) lowpass_fused_kernel(
+        const float* __restrict__ stack, int64_t num_stack, const int64_t* __restrict__ sidx,
+        const uint8_t* __restrict__ flip, const float* __restrict__ gtab,
+        const float2* __restrict__ twid, float* __restrict__ xbuf, uint32_t* __restrict__ status) {
+    constexpr int N = 1 << LOGN, H = N / 2, LOGH = LOGN - 1, RS = H + 1;   // row stride (float2)
+    constexpr int NN = N * N, NQ = NN / 4;
+    constexpr int PAIRS = N * (H / 2 + 1);                   // (row, k) pairs of the real split
+    constexpr int PER = (PAIRS + NT - 1) / NT;
+    extern __shared__ float2 C[];                            // [N][H+1]
+    __shared__ float2 tw[H + 1];
+    __shared__ double red[32];
+    const int64_t img = blockIdx.x;
+    const int64_t s = sidx[img];
+    float* dst = xbuf + img * (int64_t)NN;
+    if (s < 0 || s >= num_stack) {
+        if (threadIdx.x == 0) atomicOr(status, 2u);
+        for (int p = threadIdx.x; p < NN; p += NT) dst[p] = __int_as_float(0x7fc00000);
+        return;
+    }
+    for (int k = threadIdx.x; k <= H; k += NT) tw[k] = twid[k];
+    const bool f = flip[img] != 0;
+    const float4* src = reinterpret_cast<const float4*>(stack + s * (int64_t)NN);
+    auto load = [&](int p, int& a, int& b) -> float4 {
+        const int e = 4 * p;
+        a = e >> LOGN;
+        b = e & (N - 1);
+        float4 v = src[(a * N + (f ? N - 4 - b : b)) >> 2];
+        if (f) v = make_float4(v.w, v.z, v.y, v.x);
+        return v;
+    };
+    // background statistics (reference :277-281)
+    KSum sum, sq;
+    for (int p = threadIdx.x; p < NQ; p += NT) {
+        int a, b;
+        const float4 v = load(p, a, b);
+        const float vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float bg = vv[j] * (1.0f - mask_ref(b + j, a, N));
+            sum.add(bg);
+            sq.add(bg * bg);
+        }
+    }
+    const double tot = block_sum_double<NT>((double)sum.value(), red);
+    const double tot2 = block_sum_double<NT>((double)sq.value(), red);
+    const double mean = tot / NN;
+    const float fmean = (float)mean;
+    const float inv = (float)(1.0 / sqrt(fmax(tot2 / NN - mean * mean, 0.0)));
+    // normalised storage-orientation rows as packed complex pairs
+    for (int p = threadIdx.x; p < NQ; p += NT) {
+        int a, b;
+        const float4 v = load(p, a, b);
+        float2* row = C + a * RS + (b >> 1);
+        row[0] = make_float2((v.x - fmean) * inv, (v.y - fmean) * inv);
+        row[1] = make_float2((v.z - fmean) * inv, (v.w - fmean) * inv);
+    }
+    __syncthreads();
+    // rows: length-H complex FFT, then the real split X[k], k = 0..H
+    fft_dif<NT>(C, LOGH, N, RS, 1, tw, LOGN, false);
+    {
+        float2 o0[PER], o1[PER];
+#pragma unroll
+        for (int u = 0; u < PER; ++u) {
+            const int t = threadIdx.x + u * NT;
+            if (t >= PAIRS) break;
+            const int r = t / (H / 2 + 1), k = t - r * (H / 2 + 1);
+            const float2* row = C + r * RS;
+            const float2 zk = row[bitrev(k & (H - 1), LOGH)];
+            const float2 zm = row[bitrev((H - k) & (H - 1), LOGH)];
+            // X[k] = (zk + conj zm)/2 - i w_k (zk - conj zm)/2,  w_k = exp(-2 pi i k / N)
+            const float2 e = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
+            const float2 d = make_float2(0.5f * (zk.x - zm.x), 0.5f * (zk.y + zm.y));
+            const float2 wd = cmul(tw[k], d);
+            o0[u] = make_float2(e.x + wd.y, e.y - wd.x);
+            // X[H-k] from the same pair: (zm + conj zk)/2 - i w_{H-k} (zm - conj zk)/2
+            const float2 e2 = make_float2(0.5f * (zm.x + zk.x), 0.5f * (zm.y - zk.y));
+            const float2 d2 = make_float2(0.5f * (zm.x - zk.x), 0.5f * (zm.y + zk.y));
+            const float2 wd2 = cmul(tw[H - k], d2);
+            o1[u] = make_float2(e2.x + wd2.y, e2.y - wd2.x);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int u = 0; u < PER; ++u) {
+            const int t = threadIdx.x + u * NT;
+            if (t >= PAIRS) break;
+            const int r = t / (H / 2 + 1), k = t - r * (H / 2 + 1);
+            float2* row = C + r * RS;
+            row[k] = o0[u];
+            row[H - k] = o1[u];
+        }
+        __syncthreads();
+    }
+    // columns: length-N complex FFT (rows come out bit-reversed), multiply by G/N^2, inverse
+    fft_dif<NT>(C, LOGN, RS, 1, RS, tw, LOGN, true);
+    for (int e = threadIdx.x; e < N * RS; e += NT) {
+        const int i = e / RS, kc = e - i * RS;
+        const float g = gtab[bitrev(i, LOGN) * RS + kc];
+        C[e] = make_float2(C[e].x * g, C[e].y * g);
+    }
+    __syncthreads();
+    fft_dit_inv<NT>(C, LOGN, RS, 1, RS, tw, LOGN, true);
+    // rows: inverse real split Z[k] = (X[k] + conj X[H-k]) + i conj(w_k)(X[k] - conj X[H-k]),
+    // stored bit-reversed for the inverse DIT, then the length-H inverse FFT
+    {
+        float2 o0[PER], o1[PER];
+#pragma unroll
+        for (int u = 0; u < PER; ++u) {
+            const int t = threadIdx.x + u * NT;
+            if (t >= PAIRS) break;
+            const int r = t / (H / 2 + 1), k = t - r * (H / 2 + 1);
+            const float2* row = C + r * RS;
+            const float2 xk = row[k], xm = row[H - k];
+            const float2 e = make_float2(xk.x + xm.x, xk.y - xm.y);
+            const float2 d = make_float2(xk.x - xm.x, xk.y + xm.y);
+            const float2 wd = cmulc(d, tw[k]);
+            o0[u] = make_float2(e.x - wd.y, e.y + wd.x);
+            const float2 e2 = make_float2(xm.x + xk.x, xm.y - xk.y);
+            const float2 d2 = make_float2(xm.x - xk.x, xm.y + xk.y);
+            const float2 wd2 = cmulc(d2, tw[H - k]);
+            o1[u] = make_float2(e2.x - wd2.y, e2.y + wd2.x);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int u = 0; u < PER; ++u) {
+            const int t = threadIdx.x + u * NT;
+            if (t >= PAIRS) break;
+            const int r = t / (H / 2 + 1), k = t - r * (H / 2 + 1);
+            float2* row = C + r * RS;
+            if (k < H) row[bitrev(k, LOGH)] = o0[u];
+            if (k > 0 && k < H) row[bitrev(H - k, LOGH)] = o1[u];
+        }
+        __syncthreads();
+    }
+    fft_dit_inv<NT>(C, LOGH, N, RS, 1, tw, LOGN, false);
+    for (int p = threadIdx.x; p < N * H; p += NT) {
+        const int a = p >> LOGH, j = p & (H - 1);
+        reinterpret_cast<float2*>(dst)[p] = C[a * RS + j];
     }
 }
 
@@ -352,6 +616,84 @@ __global__ void __launch_bounds__(NT) rotate_kernel(
     for (int r = r0; r < N; r += R, X += dX, Y += dY) out[r * N + c] = sample_at(s, N, P, X, Y);
 }
 
+// Boxes too large for the shared-memory kernel (N > 236): the same two rotations with the spline
+// coefficients in global memory (the image's own workspace slots, L1/L2-resident while the CTA
+// works on them).  A = the image's spectrum slot (free at this point, >= N*N floats), B = its
+// xbuf slot.  Row stride N, no halo: every tap index is wrapped.
+__device__ __forceinline__ float sample_wrap(const float* s, int N, int64_t X, int64_t Y) {
+    const int ix = (int)(X >> 32), iy = (int)(Y >> 32);
+    const float tx = (float)(uint32_t)(X & 0xffffffffll) * 2.3283064365386963e-10f;
+    const float ty = (float)(uint32_t)(Y & 0xffffffffll) * 2.3283064365386963e-10f;
+    float wx[4], wy[4];
+    bspline_w(tx, wx);
+    bspline_w(ty, wy);
+    int cols[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) cols[j] = wrapN(iy - 1 + j, N);
+    float acc = 0.f;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const float* row = s + wrapN(ix - 1 + i, N) * N;
+        const float v = wy[0] * row[cols[0]] + wy[1] * row[cols[1]] + wy[2] * row[cols[2]] +
+                        wy[3] * row[cols[3]];
+        acc = fmaf(wx[i], v, acc);
+    }
+    return acc;
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NT) rotate_global_kernel(
+        float* __restrict__ xbuf, float2* __restrict__ spec, int64_t Kc, float* __restrict__ img_out,
+        const double* __restrict__ psi_rad, const PdDev* __restrict__ pds,
+        const int32_t* __restrict__ img_pd, int N, int nseg, float inv1mzN) {
+    __shared__ RotConst rot[2];
+    const int64_t img = blockIdx.x;
+    const int NN = N * N;
+    float* B = xbuf + img * (int64_t)NN;
+    float* A = reinterpret_cast<float*>(spec + img * Kc);
+    if (threadIdx.x == 0) {
+        const double ang = -(180.0 / 3.141592653589793) * psi_rad[img];
+        const double t = ang * (3.141592653589793 / 180.0);
+        rot[0] = make_rot(cos(t), sin(t), N);
+        const PdDev& pd = pds[img_pd[img]];
+        rot[1] = make_rot(pd.rot2_cos, pd.rot2_sin, N);
+    }
+    for (int p = threadIdx.x; p < NN; p += NT) {          // masked, back to reference orientation
+        const int r = p / N, c = p - r * N;
+        A[p] = B[c * N + r] * mask_ref(r, c, N);
+    }
+    __syncthreads();
+    prefilter_axis<NT>(A, N, N, 0, nseg, inv1mzN, false);
+    prefilter_axis<NT>(A, N, N, 1, nseg, inv1mzN, false);
+    const int R = NT / N;
+    const int c = threadIdx.x % N, r0 = threadIdx.x / N;
+    const bool active = r0 < R;
+    {
+        const RotConst Q = rot[0];
+        int64_t X = Q.bx + (int64_t)r0 * Q.rc + (int64_t)c * Q.rs;
+        int64_t Y = Q.by - (int64_t)r0 * Q.rs + (int64_t)c * Q.rc;
+        const int64_t dX = (int64_t)R * Q.rc, dY = -(int64_t)R * Q.rs;
+        if (active)
+            for (int r = r0; r < N; r += R, X += dX, Y += dY) B[r * N + c] = sample_wrap(A, N, X, Y);
+    }
+    __syncthreads();
+    prefilter_axis<NT>(B, N, N, 0, nseg, inv1mzN, false);
+    prefilter_axis<NT>(B, N, N, 1, nseg, inv1mzN, false);
+    float* out = (img_out + img * (int64_t)NN == B) ? A : img_out + img * (int64_t)NN;
+    {
+        const RotConst Q = rot[1];
+        int64_t X = Q.bx + (int64_t)r0 * Q.rc + (int64_t)c * Q.rs;
+        int64_t Y = Q.by - (int64_t)r0 * Q.rs + (int64_t)c * Q.rc;
+        const int64_t dX = (int64_t)R * Q.rc, dY = -(int64_t)R * Q.rs;
+        if (active)
+            for (int r = r0; r < N; r += R, X += dX, Y += dY) out[r * N + c] = sample_wrap(B, N, X, Y);
+    }
+    if (out == A) {
+        __syncthreads();
+        for (int p = threadIdx.x; p < NN; p += NT) B[p] = A[p];
+    }
+}
+
 // ------------------------------------------------------------------------------------------
 // CTF (ctemh_cryoFrank.py:24-44, called at :337-339) with an exact phase.
 //   CTF = sin(wr) - A cos(wr) = sqrt(1 + A^2) sin(wr - atan A),   k^2 = m / (N pix)^2,
@@ -391,30 +733,31 @@ __global__ void __launch_bounds__(256) pd_sums_kernel(
         const SumItem* __restrict__ items, float* __restrict__ partial, int N, int Nh, int64_t Kc,
         CtfConst cc) {
     const int64_t k = blockIdx.y * 256ll + threadIdx.x;
-    if (k >= Kc) return;
     const SumItem it = items[blockIdx.x];
-    const int ka = (int)(k / Nh), kb = (int)(k - (int64_t)ka * Nh);
-    const int fa = min(ka, N - ka);
-    const int m = fa * fa + kb * kb;
-    KSum s0, s1, s2, s3, s4, s5;
-    for (int64_t i = it.img_begin; i < it.img_end; ++i) {
-        const float2 F = spec[i * Kc + k];
-        int sg;
-        const float C = ctf_eval(m, qfix[i], cc, &sg);
-        s0.add(C * C);
-        s1.add(C * F.x);
-        s2.add(C * F.y);
-        s3.add(sg > 0 ? F.x : (sg < 0 ? -F.x : 0.f));
-        s4.add(sg > 0 ? F.y : (sg < 0 ? -F.y : 0.f));
-        s5.add(F.x * F.x + F.y * F.y);
+    if (k < Kc) {
+        const int ka = (int)(k / Nh), kb = (int)(k - (int64_t)ka * Nh);
+        const int fa = min(ka, N - ka);
+        const int m = fa * fa + kb * kb;
+        KSum s0, s1, s2, s3, s4, s5;
+        for (int64_t i = it.img_begin; i < it.img_end; ++i) {
+            const float2 F = spec[i * Kc + k];
+            int sg;
+            const float C = ctf_eval(m, qfix[i], cc, &sg);
+            s0.add(C * C);
+            s1.add(C * F.x);
+            s2.add(C * F.y);
+            s3.add(sg > 0 ? F.x : (sg < 0 ? -F.x : 0.f));
+            s4.add(sg > 0 ? F.y : (sg < 0 ? -F.y : 0.f));
+            s5.add(F.x * F.x + F.y * F.y);
+        }
+        float* out = partial + (int64_t)blockIdx.x * 6 * Kc + k;
+        out[0 * Kc] = s0.value();
+        out[1 * Kc] = s1.value();
+        out[2 * Kc] = s2.value();
+        out[3 * Kc] = s3.value();
+        out[4 * Kc] = s4.value();
+        out[5 * Kc] = s5.value();
     }
-    float* out = partial + (int64_t)blockIdx.x * 6 * Kc + k;
-    out[0 * Kc] = s0.value();
-    out[1 * Kc] = s1.value();
-    out[2 * Kc] = s2.value();
-    out[3 * Kc] = s3.value();
-    out[4 * Kc] = s4.value();
-    out[5 * Kc] = s5.value();
 }
 
 // 5. finalize: FP64 sum over the PD's items; centring vectors, average spectra, scale
@@ -468,12 +811,16 @@ __global__ void __launch_bounds__(256) pd_finalize_kernel(
 //   Features are written scaled by the PD's power of two; a_i in FP64 unscaled.
 //   The spectrum is overwritten with sign(C) F / N^2 (input of the phase-flip inverse FFT).
 // ------------------------------------------------------------------------------------------
-template <bool SPLIT>
+// MODE 0: FP32 features; 1: bf16 hi/lo.  Frequency slot k (k >= Kc: zero padding) goes to
+// feature column colmap[k]: 64-wide chunks ordered so the dominant low frequencies are
+// accumulated last (radius_descending_columns).
+template <int MODE>
 __global__ void __launch_bounds__(256) features_kernel(
         float2* __restrict__ spec, const uint64_t* __restrict__ qfix,
         const PdDev* __restrict__ pds, const int32_t* __restrict__ img_pd,
-        const int32_t* __restrict__ img_row, const float* __restrict__ means,
-        const uint32_t* __restrict__ pd_max, void* __restrict__ feat_a, void* __restrict__ feat_b,
+        const int32_t* __restrict__ img_row, const int32_t* __restrict__ colmap,
+        const float* __restrict__ means,
+        const uint32_t* __restrict__ scale_bits, void* __restrict__ feat_a, void* __restrict__ feat_b,
         double* __restrict__ pair_norm, float* __restrict__ ctf_out,
         float2* __restrict__ spectrum_out, int N, int Nh, int64_t Kc, int64_t Kc_pad,
         int64_t mstride, CtfConst cc) {
@@ -482,7 +829,7 @@ __global__ void __launch_bounds__(256) features_kernel(
     const int pd = img_pd[img];
     const int64_t row = img_row[img];
     const float* mu = means + pd * mstride;
-    const float sc = feature_scale_from_bits(pd_max[pd]);
+    const float sc = feature_scale_from_bits(scale_bits[pd]);
     const uint64_t qf = qfix[img];
     const float inv_nn = 1.0f / ((float)N * (float)N);
     const int64_t K4 = 4 * Kc_pad;
@@ -490,6 +837,7 @@ __global__ void __launch_bounds__(256) features_kernel(
     KSum acc;
     for (int64_t k = threadIdx.x; k < Kc_pad; k += 256) {
         float fu = 0.f, fv = 0.f, fr = 0.f, fs = 0.f;
+        const int64_t col = colmap[k];
         if (k < Kc) {
             const int ka = (int)(k / Nh), kb = (int)(k - (int64_t)ka * Nh);
             const int fa = min(ka, N - ka);
@@ -516,22 +864,20 @@ __global__ void __launch_bounds__(256) features_kernel(
             const float sgf = (float)sg * inv_nn;
             sp[k] = make_float2(sgf * F.x, sgf * F.y);
         }
-        if (SPLIT) {
+        const float vals[4] = {fu, fv, fr, fs};
+        if (MODE == 1) {
             __nv_bfloat16* hi = (__nv_bfloat16*)feat_a + row * K4;
             __nv_bfloat16* lo = (__nv_bfloat16*)feat_b + row * K4;
-            const float vals[4] = {fu, fv, fr, fs};
 #pragma unroll
             for (int b = 0; b < 4; ++b) {
                 const __nv_bfloat16 h = __float2bfloat16_rn(vals[b]);
-                hi[b * Kc_pad + k] = h;
-                lo[b * Kc_pad + k] = __float2bfloat16_rn(vals[b] - __bfloat162float(h));
+                hi[b * Kc_pad + col] = h;
+                lo[b * Kc_pad + col] = __float2bfloat16_rn(vals[b] - __bfloat162float(h));
             }
         } else {
             float* x = (float*)feat_a + row * K4;
-            x[k] = fu;
-            x[Kc_pad + k] = fv;
-            x[2 * Kc_pad + k] = fr;
-            x[3 * Kc_pad + k] = fs;
+#pragma unroll
+            for (int b = 0; b < 4; ++b) x[b * Kc_pad + col] = vals[b];
         }
     }
     const double a = block_sum_double<256>((double)acc.value(), red);
@@ -583,8 +929,12 @@ namespace kern {
 int gather_normalize(const mem_plan& P, const mem_inputs& in, float* xbuf, uint32_t* status,
                      cudaStream_t s) {
     if (P.n_images == 0) return MEM_OK;
-    gather_normalize_kernel<256><<<(unsigned)P.n_images, 256, 0, s>>>(
-        in.stack, in.num_stack, in.stack_index, in.flip, xbuf, P.N, status);
+    if (P.N % 4 == 0)
+        gather_normalize_v4_kernel<256><<<(unsigned)P.n_images, 256, 0, s>>>(
+            in.stack, in.num_stack, in.stack_index, in.flip, xbuf, P.N, status);
+    else
+        gather_normalize_kernel<256><<<(unsigned)P.n_images, 256, 0, s>>>(
+            in.stack, in.num_stack, in.stack_index, in.flip, xbuf, P.N, status);
     MEM_LAUNCH_CHECK();
     return MEM_OK;
 }
@@ -602,10 +952,50 @@ int lowpass(const mem_plan& P, float2* spec, float* gtab, cudaStream_t s) {
     return MEM_OK;
 }
 
+bool lowpass_fused_supported(const mem_plan& P) {
+    const int N = P.N;
+    return N >= 16 && N <= 128 && (N & (N - 1)) == 0;
+}
+
+int lowpass_fused(const mem_plan& P, const mem_inputs& in, const float* gtab,
+                  const float2* twid, float* xbuf, uint32_t* status, cudaStream_t s) {
+    if (P.n_images == 0) return MEM_OK;
+    constexpr int NT = 512;
+    const size_t smem = (size_t)P.N * (P.N / 2 + 1) * sizeof(float2);
+#define MEM_LPF(LOGN)                                                                              do {                                                                                               MEM_CUDA_TRY(cudaFuncSetAttribute(lowpass_fused_kernel<NT, LOGN>,                                                                cudaFuncAttributeMaxDynamicSharedMemorySize,                                                   (int)smem));                                                 lowpass_fused_kernel<NT, LOGN><<<(unsigned)P.n_images, NT, smem, s>>>(                             in.stack, in.num_stack, in.stack_index, in.flip, gtab, twid, xbuf, status);            } while (0)
+    switch (P.N) {
+        case 16: MEM_LPF(4); break;
+        case 32: MEM_LPF(5); break;
+        case 64: MEM_LPF(6); break;
+        case 128: MEM_LPF(7); break;
+        default: return MEM_ERR_UNSUPPORTED;
+    }
+#undef MEM_LPF
+    MEM_LAUNCH_CHECK();
+    return MEM_OK;
+}
+
+int lowpass_table(const mem_plan& P, float* gtab, cudaStream_t s) {
+    const int KcN = P.N * P.Nh;
+    lowpass_table_kernel<<<(KcN + 255) / 256, 256, 0, s>>>(
+        gtab, P.N, P.Nh, P.params.filter_type, P.params.filter_Qc, P.params.filter_order);
+    MEM_LAUNCH_CHECK();
+    return MEM_OK;
+}
+
 int rotate(const mem_plan& P, const mem_inputs& in, float* xbuf, float* img_out,
-           const PdDev* pd_table, const int32_t* img_pd, cudaStream_t s) {
+           const PdDev* pd_table, const int32_t* img_pd, float2* spec, cudaStream_t s) {
     if (P.n_images == 0) return MEM_OK;
     const int N = P.N;
+    if (N > kMaxSmemN) {
+        constexpr int NT = 512;
+        const int nseg = std::max(1, std::min(NT / N, N / 16));
+        rotate_global_kernel<NT><<<(unsigned)P.n_images, NT, 0, s>>>(
+            xbuf, spec, P.Kc, img_out, in.psi_rad, pd_table, img_pd, N, nseg,
+            (float)(1.0 / (1.0 - std::pow((double)kZ1, (double)N))));
+        MEM_LAUNCH_CHECK();
+        return MEM_OK;
+    }
     const int Pst = ((N + 3) % 2 == 0) ? N + 4 : N + 3;     // odd row stride, 3-px halo
     const size_t smem = (size_t)(N + 3) * Pst * sizeof(float);
     constexpr int NT = 512;
@@ -660,18 +1050,19 @@ int pd_finalize(const mem_plan& P, const float* partial, const SumItem* items,
 }
 
 int features(const mem_plan& P, float2* spec, const uint64_t* qf, const PdDev* pds,
-             const int32_t* img_pd, const int32_t* img_row, const float* means,
-             const uint32_t* pd_max, void* feat_a, void* feat_b, double* pair_norm,
-             float* ctf_out, float* spectrum_out, cudaStream_t s) {
+             const int32_t* img_pd, const int32_t* img_row, const int32_t* colmap,
+             const float* means, const uint32_t* scale_bits, void* feat_a, void* feat_b,
+             double* pair_norm, float* ctf_out, float* spectrum_out, cudaStream_t s) {
     if (P.n_images == 0) return MEM_OK;
+#define MEM_FEATS(MODE)                                                                        \
+    features_kernel<MODE><<<(unsigned)P.n_images, 256, 0, s>>>(                                \
+        spec, qf, pds, img_pd, img_row, colmap, means, scale_bits, feat_a, feat_b, pair_norm,  \
+        ctf_out, (float2*)spectrum_out, P.N, P.Nh, P.Kc, P.Kc_pad, means_stride(P), P.ctf)
     if (P.params.precision == MEM_PREC_SPLIT_BF16)
-        features_kernel<true><<<(unsigned)P.n_images, 256, 0, s>>>(
-            spec, qf, pds, img_pd, img_row, means, pd_max, feat_a, feat_b, pair_norm, ctf_out,
-            (float2*)spectrum_out, P.N, P.Nh, P.Kc, P.Kc_pad, means_stride(P), P.ctf);
+        MEM_FEATS(1);
     else
-        features_kernel<false><<<(unsigned)P.n_images, 256, 0, s>>>(
-            spec, qf, pds, img_pd, img_row, means, pd_max, feat_a, feat_b, pair_norm, ctf_out,
-            (float2*)spectrum_out, P.N, P.Nh, P.Kc, P.Kc_pad, means_stride(P), P.ctf);
+        MEM_FEATS(0);
+#undef MEM_FEATS
     MEM_LAUNCH_CHECK();
     return MEM_OK;
 }

@@ -73,7 +73,7 @@ def test_invalid_arguments(lib):
     P = StageParams(N=64, pix_size=2.0, Cs=2.7, EkV=300.0, AmpContrast=0.1).to_c()
     assert _plan(lib, P, [0], [1.0])[0] == _lib.MEM_ERR_INVALID
     assert _plan(lib, P, [5], [float('nan')])[0] == _lib.MEM_ERR_INVALID
-    big = StageParams(N=250, pix_size=2.0, Cs=2.7, EkV=300.0, AmpContrast=0.1).to_c()
+    big = StageParams(N=520, pix_size=2.0, Cs=2.7, EkV=300.0, AmpContrast=0.1).to_c()
     assert _plan(lib, big, [5], [1.0])[0] == _lib.MEM_ERR_UNSUPPORTED
     bad = StageParams(N=64, pix_size=-1.0, Cs=2.7, EkV=300.0, AmpContrast=0.1).to_c()
     assert _plan(lib, bad, [5], [1.0])[0] == _lib.MEM_ERR_INVALID

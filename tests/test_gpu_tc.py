@@ -62,11 +62,13 @@ def test_tc_single_tile(cuda_ready):
     cfg, ds = _dataset(32, 24, conj=1.0)
     r32 = _run(torch, cfg, ds, 'fp32')
     rtc = _run(torch, cfg, ds, 'bf16x3')
+    r4 = _run(torch, cfg, ds, 'bf16x3', env={'MEM_TC_TERMS': 4})
     D64 = _d64(cfg, ds, r32)
-    e32, etc = rel(r32['D'], D64), rel(rtc['D'], D64)
-    print('single tile: fp32 %.3g  bf16x3 %.3g' % (e32, etc))
+    e32, etc, e4 = rel(r32['D'], D64), rel(rtc['D'], D64), rel(r4['D'], D64)
+    print('single tile: fp32 %.3g  bf16x3 %.3g  bf16x4 %.3g' % (e32, etc, e4))
     np.testing.assert_array_equal(rtc['D'], rtc['D'].T)
     assert etc < 1e-6, etc
+    assert e4 < 1e-6, e4
 
 
 def test_tc_multi_tile_ragged(cuda_ready):
@@ -88,12 +90,14 @@ def test_tc_multi_tile_ragged(cuda_ready):
         assert rel(b['D'], a['D']) < 2e-6
 
 
-@pytest.mark.parametrize('group,kahan', [(0, 0), (1, 0), (2, 0), (4, 0), (2, 1), (8, 1)])
-def test_tc_accumulation_groups(cuda_ready, group, kahan):
+@pytest.mark.parametrize('terms', [3, 4])
+@pytest.mark.parametrize('group,kahan', [(0, 0), (1, 0), (2, 0), (4, 0), (1, 1), (4, 1)])
+def test_tc_accumulation_groups(cuda_ready, group, kahan, terms):
     """Near-duplicate images (cancellation) at 128 px: error of each accumulation setting."""
     torch = cuda_ready
     cfg, ds = _dataset(128, 384, near_dup=0.05, seed=9)
-    rtc = _run(torch, cfg, ds, 'bf16x3', env={'MEM_TC_GROUP_CHUNKS': group, 'MEM_TC_KAHAN': kahan})
+    rtc = _run(torch, cfg, ds, 'bf16x3', env={'MEM_TC_GROUP_CHUNKS': group, 'MEM_TC_KAHAN': kahan,
+                                             'MEM_TC_TERMS': terms})
     D64 = _d64(cfg, ds, rtc)
     e = rel(rtc['D'], D64)
     nd = np.nonzero(ds.near_dup_of >= 0)[0]
@@ -101,6 +105,32 @@ def test_tc_accumulation_groups(cuda_ready, group, kahan):
     pos = {int(v): i for i, v in enumerate(ds.CG[0])}
     pairs = [(pos[int(a)], pos[int(b)]) for a, b in zip(nd, src) if int(a) in pos and int(b) in pos]
     elem = max(abs(rtc['D'][i, j] - D64[i, j]) / D64[i, j] for i, j in pairs) if pairs else 0.0
-    print('group=%d kahan=%d: normwise %.3g, near-duplicate elementwise %.3g' % (group, kahan, e, elem))
-    if (group, kahan) == (2, 1):      # the default setting
+    print('terms=%d group=%d kahan=%d: normwise %.3g, near-duplicate elementwise %.3g'
+          % (terms, group, kahan, e, elem))
+    if (group, kahan) == (1, 0):        # the default accumulation setting
         assert e < 1e-6
+
+
+@pytest.mark.parametrize('N', [32, 64, 128])
+def test_fused_lowpass_matches_cufft_path(cuda_ready, N):
+    """The shared-memory FFT low-pass (power-of-two N) against the cuFFT path, same inputs."""
+    torch = cuda_ready
+    cfg, ds = _dataset(N, 40, conj=0.5, seed=44 + N)
+    outs = {}
+    for fused in (0, 1):
+        from manifoldem_python_gb300.pipeline import DistanceStage, PdJob, StageParams
+        old = os.environ.get('MEM_FUSED_LOWPASS')
+        os.environ['MEM_FUSED_LOWPASS'] = str(fused)
+        try:
+            st = DistanceStage(StageParams(N=cfg.N, pix_size=cfg.pix, Cs=cfg.cs, EkV=cfg.kv,
+                                           AmpContrast=cfg.ampc))
+            ind = ds.CG[0]
+            outs[fused] = st.run([PdJob(ind=ind, q=ds.q[:, ind], df=ds.df[ind])],
+                                 ds.stack.to('cuda'), ds.nStot, outputs=('D', 'img_all'))[0]
+        finally:
+            if old is None:
+                os.environ.pop('MEM_FUSED_LOWPASS', None)
+            else:
+                os.environ['MEM_FUSED_LOWPASS'] = old
+    assert rel(outs[1]['img_all'], outs[0]['img_all']) < 2e-6
+    assert rel(outs[1]['D'], outs[0]['D']) < 2e-6
