@@ -178,13 +178,16 @@ def choose_sample(counts, cores, max_n):
 
 # ------------------------------------------------------------------------------- GPU side
 def kernels_per_execute(outputs, avg_only, N):
-    """Kernels of this library one mem_plan_execute launches (cuFFT kernels excluded):
-    lowpass_table and either lowpass_fused (power-of-two N <= 128) or gather_normalize +
-    lowpass_apply, then rotate, qfix, pd_sums, pd_finalize, features, [avg_store],
-    [intensity], [contraction]."""
-    fused = (N & (N - 1)) == 0 and 16 <= N <= 128 and os.environ.get('MEM_FUSED_LOWPASS', '0') != '0'
-    k = 7 if fused else 8
+    """Kernels of this library one mem_plan_execute launches (cuFFT kernels excluded).
+    N = 32, 64, 128 (shared-memory FFTs): lowpass_table, lowpass_fft, rotate, spectrum_fft,
+    qfix, pd_sums, pd_finalize, features, [inverse_fft + avg_store], [inverse_fft + intensity],
+    [contraction].  Other N (cuFFT transforms): lowpass_table, gather_normalize, lowpass_apply,
+    rotate, qfix, pd_sums, pd_finalize, features, [avg_store], [intensity], [contraction]."""
+    smem = N in (32, 64, 128) and os.environ.get('MEM_SMEM_FFT', '1') != '0'
+    k = 8
     if 'img_avg' in outputs or 'img_avg_flip' in outputs:
+        k += 2 if smem else 1
+    if smem and ('img_all_intensity' in outputs or 'img_all_flip' in outputs):
         k += 1
     if 'img_all_intensity' in outputs:
         k += 1
@@ -257,14 +260,27 @@ def run_gpu(args, rank, world):
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize(dev)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # an image stack smaller than twice L2 could stay cached between steps: then every step is
+    # timed alone, after a write of a buffer larger than L2 outside its event pair
+    flush = stack.numel() * stack.element_size() < 2 * L2_BYTES
+    scrub = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev) if flush else None
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps if flush else 1)]
     with ClockSampler(dev.index) as clk:
-        e0.record(stream)
-        for _ in range(args.steps):
-            step()
-        e1.record(stream)
+        if flush:
+            for e0, e1 in ev:
+                scrub.fill_(1.0)
+                e0.record(stream)
+                step()
+                e1.record(stream)
+        else:
+            ev[0][0].record(stream)
+            for _ in range(args.steps):
+                step()
+            ev[0][1].record(stream)
         torch.cuda.synchronize(dev)
-    ms = e0.elapsed_time(e1) / args.steps
+    ms = sum(e0.elapsed_time(e1) for e0, e1 in ev) / args.steps
+    del scrub
     if world > 1:
         t = torch.tensor([ms], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -281,8 +297,9 @@ def run_gpu(args, rank, world):
     lib.mem_plan_set_timing(plan.handle, 0)
     phases = {lib.mem_phase_name(i).decode(): float(phase_ms[i]) for i in range(9)}
 
-    # end to end through the C ABI with host buffers
+    # end to end through the public API with host buffers
     e2e = None
+    n_pairs, n_images, graph_used = plan.n_pairs, plan.n_images, graph is not None
     if not args.no_e2e:
         pin = True
         try:
@@ -290,21 +307,42 @@ def run_gpu(args, rank, world):
         except RuntimeError:
             stack_h, pin = torch.empty(stack.shape, dtype=stack.dtype), False
         stack_h.copy_(stack)
-        meta_h = [torch.from_numpy(x).pin_memory() if pin else torch.from_numpy(x)
-                  for x in (sidx_h, flip_h, psi_h, df_h)]
-        res_names = [k for k in ('D', 'img_avg', 'img_avg_flip', 'img_all_intensity') if k in outs]
-        res_h = {k: torch.empty(outs[k].shape, dtype=outs[k].dtype, pin_memory=pin)
-                 for k in res_names}
-        h2d = stack_h.numel() * 4 + sum(m.numel() * m.element_size() for m in meta_h)
-        d2h = sum(v.numel() * v.element_size() for v in res_h.values())
+        res_names = tuple(k for k in ('D', 'img_avg', 'img_avg_flip', 'img_all_intensity')
+                          if k in outs)
+        if args.e2e_mode == 'streamed' and pin:
+            # the stack stays in pinned host memory; per group of PDs the load kernel reads its
+            # images over the host link while the previous group computes (StreamedStage)
+            from manifoldem_python_gb300.pipeline import StreamedStage
+            del graph, outs, plan
+            ds.stack = stack_h          # later host-side uses read the pinned copy
+            del stack
+            torch.cuda.empty_cache()
+            st = StreamedStage(params, counts, [g.psi_p for g in geoms], n_groups=args.e2e_groups,
+                               outputs=res_names, device=dev)
+            st.set_metadata(sidx_h, flip_h, psi_h, df_h)
+            h2d = stack_h.numel() * 4 + st.metadata_bytes()
+            d2h = st.result_bytes()
 
-        def e2e_step():
-            stack.copy_(stack_h, non_blocking=True)
-            for dst, src in zip((sidx, flip, psi, dfd), meta_h):
-                dst.copy_(src, non_blocking=True)
-            plan.execute(stack, sidx, flip, psi, dfd, outs, stream)
-            for k in res_names:
-                res_h[k].copy_(outs[k], non_blocking=True)
+            def e2e_step():
+                st.run(stack_h)
+            mode = 'streamed: stack in pinned host memory read by the load kernels over the host ' \
+                   'link, %d PD groups on load / compute / copy streams' % len(st.groups)
+        else:
+            meta_h = [torch.from_numpy(x).pin_memory() if pin else torch.from_numpy(x)
+                      for x in (sidx_h, flip_h, psi_h, df_h)]
+            res_h = {k: torch.empty(outs[k].shape, dtype=outs[k].dtype, pin_memory=pin)
+                     for k in res_names}
+            h2d = stack_h.numel() * 4 + sum(m.numel() * m.element_size() for m in meta_h)
+            d2h = sum(v.numel() * v.element_size() for v in res_h.values())
+
+            def e2e_step():
+                stack.copy_(stack_h, non_blocking=True)
+                for dst, src in zip((sidx, flip, psi, dfd), meta_h):
+                    dst.copy_(src, non_blocking=True)
+                plan.execute(stack, sidx, flip, psi, dfd, outs, stream)
+                for k in res_names:
+                    res_h[k].copy_(outs[k], non_blocking=True)
+            mode = 'copy: stack copied host to device, then one execute'
 
         e2e_step()
         torch.cuda.synchronize(dev)
@@ -318,10 +356,10 @@ def run_gpu(args, rank, world):
             t = torch.tensor([e2e_ms], device=dev)
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
             e2e_ms = float(t.item())
-        e2e = dict(ms=e2e_ms, h2d=int(h2d), d2h=int(d2h), pinned=pin)
-        del stack_h, res_h
-    return dict(ms=ms, pairs=plan.n_pairs, n_images=plan.n_images, counts=counts,
-                graph=graph is not None,
+        e2e = dict(ms=e2e_ms, h2d=int(h2d), d2h=int(d2h), pinned=pin, mode=mode)
+        del stack_h
+    return dict(ms=ms, pairs=n_pairs, n_images=n_images, counts=counts,
+                graph=graph_used, l2_flush=flush,
                 phases=phases, clocks=clk.summary(), t_gen=t_gen, e2e=e2e, ds=ds, cfg=cfg,
                 kernels=kernels_per_execute(outputs, False, cfg.N), outputs=outputs)
 
@@ -343,7 +381,7 @@ def roofline(r, args):
                     peak_source=peaks['src'] + ' bf16 sustained', algorithmic_flops=flops)
     # image-side phases: algorithmic bytes per image of the phase
     NN, Kc = N * N, N * (N // 2 + 1)
-    per_img = {'gather': 2 * 4 * NN, 'lowpass': 2 * (4 * NN + 8 * Kc), 'rotate': 4 * 4 * NN,
+    per_img = {'gather': 2 * 4 * NN, 'lowpass': 2 * (4 * NN + 8 * Kc), 'rotate': 2 * 4 * NN,
                'spectrum': 4 * NN + 8 * Kc, 'sums': 8 * Kc, 'features': 8 * Kc + 16 * Kc + 8 * Kc,
                'averages': 0, 'flip': 8 * Kc + 4 * NN, }.get(dom, 4 * NN)
     b = per_img * r['n_images']
@@ -430,6 +468,11 @@ def main():
     ap.add_argument('--outputs', default='D,img_avg,img_avg_flip,img_all_intensity')
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--no-e2e', action='store_true')
+    ap.add_argument('--e2e-mode', default='streamed', choices=['streamed', 'copy'],
+                    help='streamed: stack left in pinned host memory, PD groups pipelined over '
+                         'load / compute / copy streams; copy: one host-to-device copy of the '
+                         'stack, then one execute')
+    ap.add_argument('--e2e-groups', type=int, default=4)
     ap.add_argument('--no-precision', action='store_true',
                     help='skip the FP64 / diffusion-map precision report of one sample PD')
     ap.add_argument('--cpu-max-n', type=int, default=900)
@@ -511,7 +554,8 @@ def main():
                              '%d pairs per GPU' % (args.config, len(r['counts']), cfg.N, cfg.N,
                                                    cfg.n_median, r['n_images'], r['pairs']),
                     precision=args.precision, outputs=list(r['outputs']),
-                    l2='inputs larger than L2 (%.1f GB image stack)' % (
+                    l2=('L2 flushed before every timed step (%.2f GB image stack)'
+                        if r['l2_flush'] else 'inputs larger than L2 (%.1f GB image stack)') % (
                         r['ds'].stack.numel() * 4 / 1e9),
                     parallelism='PD-sharded, one process per GPU' if world > 1 else 'single GPU',
                     cuda_graph=r['graph']),
@@ -526,7 +570,7 @@ def main():
         e = r['e2e']
         line['e2e'] = dict(value=pairs_total / (e['ms'] * 1e-3), unit='pairs/s',
                            h2d_bytes_per_step=e['h2d'], d2h_bytes_per_step=e['d2h'],
-                           ms_per_step=e['ms'], pinned=e['pinned'])
+                           ms_per_step=e['ms'], pinned=e['pinned'], mode=e['mode'])
     if not args.no_precision:
         line['precision'] = precision_report(args, r['ds'], r['counts'], cfg, args.precision)
     if not args.no_cpu_baseline:

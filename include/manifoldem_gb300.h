@@ -75,7 +75,10 @@ typedef struct mem_params {
 /* Per-call device inputs.  Images of PD p are the pd_count[p] consecutive entries starting at
  * the sum of the previous counts, in the order of the PD's index list ``ind``.           */
 typedef struct mem_inputs {
-    const float*   stack;        /* SPIDER raw stack, num_stack * N * N float32              */
+    const float*   stack;        /* SPIDER raw stack, num_stack * N * N float32: device memory,
+                                    or host memory the GPU can read (pinned / registered, or
+                                    any host memory on a system whose GPU uses the host page
+                                    tables); only the first kernel reads it, once per image   */
     int64_t        num_stack;
     const int64_t* stack_index;  /* [n_images] stack image of each entry: ind, or
                                     ind - nStot/2 for conjugate views (reference :247-252)      */
@@ -128,6 +131,16 @@ int mem_plan_upload(mem_plan* plan, void* workspace, size_t workspace_bytes, voi
  * caller.  Stream-ordered and graph-capturable.                                            */
 int mem_plan_execute(mem_plan* plan, const mem_inputs* in, const mem_outputs* out,
                      void* workspace, size_t workspace_bytes, void* stream);
+
+/* mem_plan_execute with the one kernel that reads the stack (gather + normalisation, fused with
+ * the low-pass for N = 32, 64, 128) issued on load_stream and the rest of the stage on stream,
+ * which waits for it (an event owned by the plan).  With the stack in host memory the load
+ * kernel runs on a small grid (128 CTAs; MEM_HOST_LOAD_CTAS) at the host link's rate, so the
+ * loads of one plan overlap the computation of other plans on other streams.  The reference has
+ * no counterpart (its workers read the stack from disk, :255-283).  Not for graph capture.  */
+int mem_plan_execute_split(mem_plan* plan, const mem_inputs* in, const mem_outputs* out,
+                           void* workspace, size_t workspace_bytes, void* load_stream,
+                           void* stream);
 
 /* Reads the device status word of the workspace (after the stream has been synchronised):
  * MEM_OK, or MEM_ERR_DEVICE_TIMEOUT if a bounded device-side wait gave up.                 */

@@ -7,6 +7,7 @@ without the library raises ``LibraryNotBuilt``.
 from __future__ import annotations
 
 import ctypes
+import glob
 import os
 import shutil
 import subprocess
@@ -20,7 +21,7 @@ REPO = os.path.dirname(HERE)
 INCLUDE = os.path.join(REPO, 'include')
 BUILD_DIR = os.path.join(REPO, '_build')
 LIB_PATH = os.path.join(HERE, 'libmanifoldem_gb300.so')
-SOURCES = ['abi.cu', 'prologue.cu', 'gemm_fp32.cu', 'gemm_tc.cu', 'noalloc.cu']
+SOURCES = ['abi.cu', 'prologue.cu', 'gemm_fp32.cu', 'gemm_tc.cu', 'noalloc.cu', 'image_fft.cu']
 ARCH_FLAGS = ['-gencode', 'arch=compute_103a,code=sm_103a']
 
 # status codes (include/manifoldem_gb300.h)
@@ -65,8 +66,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
     nvcc = _nvcc()
     os.makedirs(BUILD_DIR, exist_ok=True)
     srcs = [os.path.join(CSRC, s) for s in SOURCES]
-    deps = srcs + [os.path.join(CSRC, 'mem_internal.cuh'),
-                   os.path.join(INCLUDE, 'manifoldem_gb300.h')]
+    deps = srcs + sorted(glob.glob(os.path.join(CSRC, '*.cuh'))) + [
+        os.path.join(INCLUDE, 'manifoldem_gb300.h')]
     if not force and os.path.exists(LIB_PATH):
         lib_m = os.path.getmtime(LIB_PATH)
         if all(os.path.getmtime(d) <= lib_m for d in deps):
@@ -136,6 +137,9 @@ SIGNATURES = {
     'mem_plan_upload': (c_int32, [c_void_p, c_void_p, c_size_t, c_void_p]),
     'mem_plan_execute': (c_int32, [c_void_p, ctypes.POINTER(MemInputs),
                                    ctypes.POINTER(MemOutputs), c_void_p, c_size_t, c_void_p]),
+    'mem_plan_execute_split': (c_int32, [c_void_p, ctypes.POINTER(MemInputs),
+                                         ctypes.POINTER(MemOutputs), c_void_p, c_size_t, c_void_p,
+                                         c_void_p]),
     'mem_workspace_status': (c_int32, [c_void_p, c_void_p]),
     'mem_plan_set_timing': (c_int32, [c_void_p, c_int32]),
     'mem_plan_phase_times': (c_int32, [c_void_p, ctypes.POINTER(ctypes.c_float), c_int32]),

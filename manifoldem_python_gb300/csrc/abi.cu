@@ -250,7 +250,11 @@ int mem_plan_create(const mem_params* params, int32_t n_pd, const int32_t* pd_co
     if (const char* e = std::getenv("MEM_TC_GROUP_CHUNKS")) P->tc_group_chunks = std::atoi(e);
     if (const char* e = std::getenv("MEM_TC_KAHAN")) P->tc_kahan = std::atoi(e) != 0;
     if (const char* e = std::getenv("MEM_TC_TERMS")) P->tc_lolo = std::atoi(e) >= 4;
-    if (const char* e = std::getenv("MEM_FUSED_LOWPASS")) P->fused_lowpass = std::atoi(e) != 0;
+    // image transforms: the shared-memory FFT kernels where they exist (MEM_SMEM_FFT=0 selects
+    // cuFFT, for comparison)
+    if (const char* e = std::getenv("MEM_SMEM_FFT")) P->smem_fft = std::atoi(e) != 0;
+    P->smem_fft = P->smem_fft && kern::smem_fft_supported(*P);
+    if (const char* e = std::getenv("MEM_HOST_LOAD_CTAS")) P->host_load_ctas = std::atoi(e);
 
     // cuFFT work sizes: exact when a device is current, an estimate otherwise
     std::vector<int> img_batches;
@@ -262,6 +266,7 @@ int mem_plan_create(const mem_params* params, int32_t n_pd, const int32_t* pd_co
         P->num_sms = 152;
     }
     size_t work = 0;
+    if (P->smem_fft) img_batches.clear();      // no cuFFT plan is used
     for (int b : img_batches) {
         for (cufftType ty : {CUFFT_R2C, CUFFT_C2R}) {
             if (have_dev) {
@@ -384,8 +389,38 @@ int mem_plan_upload(mem_plan* plan, void* workspace, size_t workspace_bytes, voi
     return MEM_OK;
 }
 
+namespace {
+// true when p is host memory (pinned, registered, or pageable on a system whose GPU reads host
+// page tables): the stack is then read over the host link
+bool is_host_memory(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost || a.type == cudaMemoryTypeUnregistered;
+}
+
+int execute_impl(mem_plan* plan, const mem_inputs* in, const mem_outputs* out, void* workspace,
+                 size_t workspace_bytes, cudaStream_t ls, cudaStream_t s);
+}  // namespace
+
 int mem_plan_execute(mem_plan* plan, const mem_inputs* in, const mem_outputs* out,
                      void* workspace, size_t workspace_bytes, void* stream) {
+    return execute_impl(plan, in, out, workspace, workspace_bytes, (cudaStream_t)stream,
+                        (cudaStream_t)stream);
+}
+
+int mem_plan_execute_split(mem_plan* plan, const mem_inputs* in, const mem_outputs* out,
+                           void* workspace, size_t workspace_bytes, void* load_stream,
+                           void* stream) {
+    return execute_impl(plan, in, out, workspace, workspace_bytes, (cudaStream_t)load_stream,
+                        (cudaStream_t)stream);
+}
+
+namespace {
+int execute_impl(mem_plan* plan, const mem_inputs* in, const mem_outputs* out, void* workspace,
+                 size_t workspace_bytes, cudaStream_t ls, cudaStream_t s) {
     if (!plan || !in || !out || !workspace) return MEM_ERR_INVALID;
     if (workspace_bytes < plan->lay.total) return MEM_ERR_WORKSPACE;
     if (!in->stack || !in->stack_index || !in->flip || !in->psi_rad || !in->df)
@@ -394,7 +429,10 @@ int mem_plan_execute(mem_plan* plan, const mem_inputs* in, const mem_outputs* ou
     if (plan->device < 0) return MEM_ERR_INVALID;   // not uploaded
     const mem_plan& P = *plan;
     const Layout& L = P.lay;
-    cudaStream_t s = (cudaStream_t)stream;
+    const bool split = ls != s;
+    // the stack-reading kernel of a split execute: a small grid when the stack is host memory,
+    // so that the rest of the GPU keeps computing while it waits on the host link
+    const int64_t load_ctas = (split && is_host_memory(in->stack)) ? P.host_load_ctas : 0;
     void* ws = workspace;
     uint32_t* status = at<uint32_t>(ws, L.status);
     mem_plan& PM = *plan;
@@ -403,7 +441,7 @@ int mem_plan_execute(mem_plan* plan, const mem_inputs* in, const mem_outputs* ou
     // event k marks the start of phase k; phase k ends at the next recorded event
     auto mark = [&](int phase) -> int {
         if (!PM.timing) return MEM_OK;
-        MEM_CUDA_TRY(cudaEventRecord(PM.ev[phase], s));
+        MEM_CUDA_TRY(cudaEventRecord(PM.ev[phase], phase <= 2 ? ls : s));
         if (phase > 0) PM.phase_ran[phase - 1] = true;
         return MEM_OK;
     };
@@ -423,32 +461,43 @@ int mem_plan_execute(mem_plan* plan, const mem_inputs* in, const mem_outputs* ou
         if (st != MEM_OK) return st; \
     } while (0)
 
-    MEM_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(uint32_t) * 4, s));
-    if (P.fused_lowpass && kern::lowpass_fused_supported(P)) {
+    // the stack is read by exactly one kernel (the first), issued on the load stream
+    MEM_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(uint32_t) * 4, ls));
+    MEM_STEP(mark(0));
+    MEM_STEP(kern::lowpass_table(P, at<float>(ws, L.gtab), ls));
+    if (P.smem_fft) {
         // (a2, a3) gather, flip, normalisation and low-pass in one shared-memory pass
-        MEM_STEP(mark(0));
         MEM_STEP(mark(1));
-        MEM_STEP(kern::lowpass_table(P, at<float>(ws, L.gtab), s));
         MEM_STEP(kern::lowpass_fused(P, *in, at<float>(ws, L.gtab), at<float2>(ws, L.twid), xbuf,
-                                     status, s));
-        MEM_STEP(mark(2));
+                                     status, load_ctas, ls));
     } else {
         // (a2) gather, conjugate flip, normalisation
-        MEM_STEP(mark(0));
-        MEM_STEP(kern::gather_normalize(P, *in, xbuf, status, s));
+        MEM_STEP(kern::gather_normalize(P, *in, xbuf, status, load_ctas, ls));
         MEM_STEP(mark(1));
+    }
+    if (split) {
+        if (!PM.load_done)
+            MEM_CUDA_TRY(cudaEventCreateWithFlags(&PM.load_done, cudaEventDisableTiming));
+        MEM_CUDA_TRY(cudaEventRecord(PM.load_done, ls));
+        MEM_CUDA_TRY(cudaStreamWaitEvent(s, PM.load_done, 0));
+    }
+    if (!P.smem_fft) {
         // (a3) low-pass filter: R2C, multiply by G/N^2, C2R
         MEM_STEP(exec_fft(P, CUFFT_R2C, P.n_images, NN, specN, xbuf, spec, work, s));
         MEM_STEP(kern::lowpass(P, spec, at<float>(ws, L.gtab), s));
         MEM_STEP(exec_fft(P, CUFFT_C2R, P.n_images, specN, NN, spec, xbuf, work, s));
-        MEM_STEP(mark(2));
     }
+    MEM_STEP(mark(2));
     // (a4, a6) mask and the two rotations -> imgAll
     float* img_all = out->img_all ? out->img_all : xbuf;
     MEM_STEP(kern::rotate(P, *in, xbuf, img_all, pds, img_pd, spec, s));
     MEM_STEP(mark(3));
     // (a8) F = fft2(imgAll)
-    MEM_STEP(exec_fft(P, CUFFT_R2C, P.n_images, NN, specN, img_all, spec, work, s));
+    const float2* twid = at<float2>(ws, L.twid);
+    if (P.smem_fft)
+        MEM_STEP(kern::spectrum_fft(P, P.n_images, img_all, twid, spec, s));
+    else
+        MEM_STEP(exec_fft(P, CUFFT_R2C, P.n_images, NN, specN, img_all, spec, work, s));
     MEM_STEP(mark(4));
     // (a7, a9) CTF, per-PD sums, centring vectors, average spectra
     MEM_STEP(kern::qfix(P, *in, qf, s));
@@ -466,19 +515,26 @@ int mem_plan_execute(mem_plan* plan, const mem_inputs* in, const mem_outputs* ou
     double* pair_norm = out->pair_norm ? out->pair_norm : at<double>(ws, L.pair_norm);
     const uint32_t* scale_bits = pd_max;
     MEM_STEP(kern::features(P, spec, qf, pds, img_pd, img_row, at<int32_t>(ws, L.colmap), means,
-                            scale_bits, feat_a, feat_b, pair_norm, out->ctf, out->spectrum, s));
+                            scale_bits, feat_a, feat_b, pair_norm, out->ctf, out->spectrum,
+                            !P.smem_fft && (out->img_all_flip || out->img_all_intensity), s));
     MEM_STEP(mark(6));
     // averages: one inverse transform per PD (linearity of the reference's per-image sums)
     float* avg_real = at<float>(ws, L.avg_real);
     if (out->img_avg || out->img_avg_flip) {
-        MEM_STEP(exec_fft(P, CUFFT_C2R, 2 * P.n_pd, specN, NN, avg_spec, avg_real, work, s));
+        if (P.smem_fft)
+            MEM_STEP(kern::inverse_fft(P, 2 * P.n_pd, avg_spec, twid, avg_real, nullptr, false, s));
+        else
+            MEM_STEP(exec_fft(P, CUFFT_C2R, 2 * P.n_pd, specN, NN, avg_spec, avg_real, work, s));
         MEM_STEP(kern::avg_store(P, avg_real, out->img_avg, out->img_avg_flip, s));
     }
     MEM_STEP(mark(7));
     // phase-flipped images and their mean intensity
     if (out->img_all_flip || out->img_all_intensity) {
         float* flip_imgs = out->img_all_flip ? out->img_all_flip : xbuf;
-        MEM_STEP(exec_fft(P, CUFFT_C2R, P.n_images, specN, NN, spec, flip_imgs, work, s));
+        if (P.smem_fft)
+            MEM_STEP(kern::inverse_fft(P, P.n_images, spec, twid, flip_imgs, qf, true, s));
+        else
+            MEM_STEP(exec_fft(P, CUFFT_C2R, P.n_images, specN, NN, spec, flip_imgs, work, s));
         MEM_STEP(kern::intensity(P, flip_imgs, pds, out->img_all_intensity, s));
     }
     MEM_STEP(mark(8));
@@ -496,6 +552,8 @@ int mem_plan_execute(mem_plan* plan, const mem_inputs* in, const mem_outputs* ou
 #undef MEM_STEP
     return MEM_OK;
 }
+
+}  // namespace
 
 int mem_plan_set_timing(mem_plan* plan, int enable) {
     if (!plan) return MEM_ERR_INVALID;

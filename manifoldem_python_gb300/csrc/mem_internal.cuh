@@ -51,6 +51,15 @@ struct CtfConst {
     float    env_c;        // envelope exponent per m: 1 / ((N pix)^2 2 sigma^2), 0 if none
 };
 
+// sign of the CTF at squared radius m (frequency units) for an image with defocus phase qf: the
+// sign of the 64-bit fixed-point phase P m^2 - Q m - atan(A)/2pi, whose sine (times a positive
+// amplitude) is the CTF
+__device__ __forceinline__ int ctf_sign(int m, uint64_t qf, const CtfConst& cc) {
+    const uint64_t mm = (uint64_t)m;
+    const int64_t sph = (int64_t)(cc.p_fix * (mm * mm) - qf * mm - cc.d_fix);
+    return (sph > 0) - (sph < 0);
+}
+
 struct Layout {
     size_t status, pd_table, sum_items, img_pd, img_row, tiles;
     size_t item_off, qfix, gtab, pd_max, colmap, twid;
@@ -82,15 +91,18 @@ struct mem_plan {
     int tc_group_chunks = 1;        // 64-wide K chunks per TMEM accumulation group (0 = all)
     bool tc_kahan = false;          // compensated register sums across groups
     bool tc_lolo = false;           // add the lo.lo product (4-term split)
-    bool fused_lowpass = false;     // shared-memory FFT low-pass for power-of-two N <= 128
-                                    // (measured slower than the cuFFT path: off by default)
+    bool smem_fft = true;           // shared-memory FFT kernels instead of cuFFT (N = 32, 64, 128)
+    int host_load_ctas = 128;       // grid of the stack-reading kernel when the stack is in host
+                                    // memory and the load runs on its own stream
     bool timing = false;
     bool timed_run = false;
     cudaEvent_t ev[MEM_NUM_PHASES + 1] = {};
     bool phase_ran[MEM_NUM_PHASES] = {};
+    cudaEvent_t load_done = nullptr; // end of the stack-reading phase (mem_plan_execute_split)
     ~mem_plan() {
         for (auto& e : ev)
             if (e) cudaEventDestroy(e);
+        if (load_done) cudaEventDestroy(load_done);
     }
 };
 
@@ -99,12 +111,21 @@ namespace mem {
 // ---- host launchers of the image-side kernels (prologue.cu) ------------------------------
 namespace kern {
 int gather_normalize(const mem_plan& P, const mem_inputs& in, float* xbuf, uint32_t* status,
-                     cudaStream_t s);
+                     int64_t max_ctas, cudaStream_t s);
+// multiply the half-plane spectra by the table G/N^2 written by lowpass_table
 int lowpass(const mem_plan& P, float2* spec, float* gtab, cudaStream_t s);
-bool lowpass_fused_supported(const mem_plan& P);
+bool smem_fft_supported(const mem_plan& P);
 int lowpass_table(const mem_plan& P, float* gtab, cudaStream_t s);
+// max_ctas > 0: a grid of at most max_ctas CTAs loops over the images
 int lowpass_fused(const mem_plan& P, const mem_inputs& in, const float* gtab,
-                  const float2* twid, float* xbuf, uint32_t* status, cudaStream_t s);
+                  const float2* twid, float* xbuf, uint32_t* status, int64_t max_ctas,
+                  cudaStream_t s);
+// shared-memory real 2D FFTs (N = 32, 64, 128) with the layout and scaling of a cuFFT R2C/C2R
+int spectrum_fft(const mem_plan& P, int64_t count, const float* images, const float2* twid,
+                 float2* spec, cudaStream_t s);
+// signed = the phase-flip inverse: element k of image i multiplied by sign(C_i(k)) / N^2 on load
+int inverse_fft(const mem_plan& P, int64_t count, const float2* spec, const float2* twid,
+                float* images, const uint64_t* qf, bool signed_flip, cudaStream_t s);
 int rotate(const mem_plan& P, const mem_inputs& in, float* xbuf, float* img_out,
            const PdDev* pd_table, const int32_t* img_pd, float2* spec, cudaStream_t s);
 int qfix(const mem_plan& P, const mem_inputs& in, uint64_t* qf, cudaStream_t s);
@@ -116,7 +137,8 @@ int pd_finalize(const mem_plan& P, const float* partial, const SumItem* items,
 int features(const mem_plan& P, float2* spec, const uint64_t* qf, const PdDev* pds,
              const int32_t* img_pd, const int32_t* img_row, const int32_t* colmap,
              const float* means, const uint32_t* scale_bits, void* feat_a, void* feat_b,
-             double* pair_norm, float* ctf_out, float* spectrum_out, cudaStream_t s);
+             double* pair_norm, float* ctf_out, float* spectrum_out, bool write_signed,
+             cudaStream_t s);
 int avg_store(const mem_plan& P, const float* avg_real, double* img_avg, double* img_avg_flip,
               cudaStream_t s);
 int intensity(const mem_plan& P, const float* flip_imgs, const PdDev* pds, double* out,

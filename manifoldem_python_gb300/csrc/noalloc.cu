@@ -193,7 +193,7 @@ extern "C" int mem_pd_distances_noalloc(const mem_params* params, int32_t n, con
                               at<float2>(ws, L.avg_spec), pd_max, s));
     NA_STEP(kern::features(P, spec, qf, pds, at<int32_t>(ws, L.img_pd), at<int32_t>(ws, L.img_row),
                            at<int32_t>(ws, L.colmap), means, scale_bits, at<char>(ws, L.feat_a),
-                           at<char>(ws, L.feat_b), pair_norm, nullptr, nullptr, s));
+                           at<char>(ws, L.feat_b), pair_norm, nullptr, nullptr, false, s));
     if (P.params.precision == MEM_PREC_FP32)
         NA_STEP(kern::gemm_fp32(P, at<float>(ws, L.feat_a), pair_norm, scale_bits,
                                 at<Tile>(ws, L.tiles), pds, D, s));

@@ -65,12 +65,10 @@ __device__ __forceinline__ double block_sum_double(double v, double* red) {
 // symmetric in (kx, ky), so the transpose commutes with it; the rotation kernel undoes it.
 // ------------------------------------------------------------------------------------------
 template <int NT>
-__global__ void __launch_bounds__(NT) gather_normalize_kernel(
-        const float* __restrict__ stack, int64_t num_stack, const int64_t* __restrict__ sidx,
-        const uint8_t* __restrict__ flip, float* __restrict__ xbuf, int N,
-        uint32_t* __restrict__ status) {
-    __shared__ double red[32];
-    const int64_t img = blockIdx.x;
+__device__ __forceinline__ void gather_normalize_one(
+        int64_t img, const float* __restrict__ stack, int64_t num_stack,
+        const int64_t* __restrict__ sidx, const uint8_t* __restrict__ flip,
+        float* __restrict__ xbuf, int N, uint32_t* __restrict__ status, double* red) {
     const int64_t s = sidx[img];
     const int NN = N * N;
     float* dst = xbuf + img * (int64_t)NN;
@@ -101,15 +99,26 @@ __global__ void __launch_bounds__(NT) gather_normalize_kernel(
     }
 }
 
+// one CTA per image, or a smaller grid looping over the images
+template <int NT>
+__global__ void __launch_bounds__(NT) gather_normalize_kernel(
+        const float* __restrict__ stack, int64_t num_stack, const int64_t* __restrict__ sidx,
+        const uint8_t* __restrict__ flip, float* __restrict__ xbuf, int N,
+        uint32_t* __restrict__ status, int64_t n_images) {
+    __shared__ double red[32];
+    for (int64_t img = blockIdx.x; img < n_images; img += gridDim.x) {
+        __syncthreads();
+        gather_normalize_one<NT>(img, stack, num_stack, sidx, flip, xbuf, N, status, red);
+    }
+}
+
 // float4 variant for N % 4 == 0: one 16-byte load / store per 4 pixels of a stack row; a
 // conjugate flip reverses the four lanes (the row reversal maps aligned quads to aligned quads)
 template <int NT>
-__global__ void __launch_bounds__(NT) gather_normalize_v4_kernel(
-        const float* __restrict__ stack, int64_t num_stack, const int64_t* __restrict__ sidx,
-        const uint8_t* __restrict__ flip, float* __restrict__ xbuf, int N,
-        uint32_t* __restrict__ status) {
-    __shared__ double red[32];
-    const int64_t img = blockIdx.x;
+__device__ __forceinline__ void gather_normalize_v4_one(
+        int64_t img, const float* __restrict__ stack, int64_t num_stack,
+        const int64_t* __restrict__ sidx, const uint8_t* __restrict__ flip,
+        float* __restrict__ xbuf, int N, uint32_t* __restrict__ status, double* red) {
     const int64_t s = sidx[img];
     const int NN = N * N, NQ = NN / 4;
     float4* dst = reinterpret_cast<float4*>(xbuf + img * (int64_t)NN);
@@ -155,6 +164,19 @@ __global__ void __launch_bounds__(NT) gather_normalize_v4_kernel(
     }
 }
 
+// one CTA per image, or a smaller grid looping over the images
+template <int NT>
+__global__ void __launch_bounds__(NT) gather_normalize_v4_kernel(
+        const float* __restrict__ stack, int64_t num_stack, const int64_t* __restrict__ sidx,
+        const uint8_t* __restrict__ flip, float* __restrict__ xbuf, int N,
+        uint32_t* __restrict__ status, int64_t n_images) {
+    __shared__ double red[32];
+    for (int64_t img = blockIdx.x; img < n_images; img += gridDim.x) {
+        __syncthreads();
+        gather_normalize_v4_one<NT>(img, stack, num_stack, sidx, flip, xbuf, N, status, red);
+    }
+}
+
 // ------------------------------------------------------------------------------------------
 // 2. low-pass filter table G(k)/N^2 and its application (reference :139-167, :286-293)
 // ------------------------------------------------------------------------------------------
@@ -182,216 +204,6 @@ __global__ void lowpass_apply_kernel(float2* __restrict__ spec, const float* __r
         v.x *= gv;
         v.y *= gv;
         spec[e] = v;
-    }
-}
-
-// ------------------------------------------------------------------------------------------
-// 2b. fused gather + normalisation + low-pass for power-of-two N <= 128 (one CTA per image)
-//
-// Same result as gather_normalize + cuFFT R2C + lowpass_apply + cuFFT C2R, with the image kept
-// in shared memory: a real 2D FFT (rows: length-N/2 complex FFT of the packed pairs
-// (x[2j], x[2j+1]) then the real-FFT split; columns: length-N complex FFT), the multiply by
-// G/N^2, and the inverse.  Forward transforms are radix-2 decimation-in-frequency (natural in,
-// bit-reversed out), inverse transforms decimation-in-time (bit-reversed in, natural out), so
-// no reordering pass is needed; G is read at the bit-reversed row.  Twiddles
-// exp(-2 pi i k / N), k <= N/2, come from a table computed in double on the host.
-// ------------------------------------------------------------------------------------------
-__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
-    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
-}
-__device__ __forceinline__ float2 cmulc(float2 a, float2 b) {   // a * conj(b)
-    return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
-}
-
-// radix-2 DIF over `batch` signals of length 2^logL; element (b, i) at C[b*bs + i*es]
-template <int NT>
-__device__ void fft_dif(float2* C, int logL, int batch, int bs, int es, const float2* tw, int logN,
-                        bool lanes_on_batch) {
-    const int L = 1 << logL, half = L >> 1;
-    for (int lh = logL - 1; lh >= 0; --lh) {
-        const int h = 1 << lh;
-        const int tstride = logN - lh - 1;            // twiddle index step N / (2h)
-        for (int t = threadIdx.x; t < batch * half; t += NT) {
-            int b, q;
-            if (lanes_on_batch) { b = t % batch; q = t / batch; }
-            else { b = t >> (logL - 1); q = t & (half - 1); }
-            const int j = q & (h - 1);
-            const int i0 = ((q >> lh) << (lh + 1)) + j;
-            float2* p0 = C + b * bs + i0 * es;
-            float2* p1 = p0 + h * es;
-            const float2 u = *p0, v = *p1;
-            *p0 = make_float2(u.x + v.x, u.y + v.y);
-            *p1 = cmul(make_float2(u.x - v.x, u.y - v.y), tw[j << tstride]);
-        }
-        __syncthreads();
-    }
-}
-
-// radix-2 DIT inverse (conjugate twiddles, unnormalised), bit-reversed in, natural out
-template <int NT>
-__device__ void fft_dit_inv(float2* C, int logL, int batch, int bs, int es, const float2* tw,
-                            int logN, bool lanes_on_batch) {
-    const int L = 1 << logL, half = L >> 1;
-    for (int lh = 0; lh < logL; ++lh) {
-        const int h = 1 << lh;
-        const int tstride = logN - lh - 1;
-        for (int t = threadIdx.x; t < batch * half; t += NT) {
-            int b, q;
-            if (lanes_on_batch) { b = t % batch; q = t / batch; }
-            else { b = t >> (logL - 1); q = t & (half - 1); }
-            const int j = q & (h - 1);
-            const int i0 = ((q >> lh) << (lh + 1)) + j;
-            float2* p0 = C + b * bs + i0 * es;
-            float2* p1 = p0 + h * es;
-            const float2 u = *p0;
-            const float2 v = cmulc(*p1, tw[j << tstride]);
-            *p0 = make_float2(u.x + v.x, u.y + v.y);
-            *p1 = make_float2(u.x - v.x, u.y - v.y);
-        }
-        __syncthreads();
-    }
-}
-
-__device__ __forceinline__ int bitrev(int k, int bits) { return (int)(__brev((unsigned)k) >> (32 - bits)); }
-
-template <int NT, int LOGN>
-__global__ void __launch_bounds__(NT) lowpass_fused_kernel(
-        const float* __restrict__ stack, int64_t num_stack, const int64_t* __restrict__ sidx,
-        const uint8_t* __restrict__ flip, const float* __restrict__ gtab,
-        const float2* __restrict__ twid, float* __restrict__ xbuf, uint32_t* __restrict__ status) {
-    constexpr int N = 1 << LOGN, H = N / 2, LOGH = LOGN - 1, RS = H + 1;   // row stride (float2)
-    constexpr int NN = N * N, NQ = NN / 4;
-    constexpr int PAIRS = N * (H / 2 + 1);                   // (row, k) pairs of the real split
-    constexpr int PER = (PAIRS + NT - 1) / NT;
-    extern __shared__ float2 C[];                            // [N][H+1]
-    __shared__ float2 tw[H + 1];
-    __shared__ double red[32];
-    const int64_t img = blockIdx.x;
-    const int64_t s = sidx[img];
-    float* dst = xbuf + img * (int64_t)NN;
-    if (s < 0 || s >= num_stack) {
-        if (threadIdx.x == 0) atomicOr(status, 2u);
-        for (int p = threadIdx.x; p < NN; p += NT) dst[p] = __int_as_float(0x7fc00000);
-        return;
-    }
-    for (int k = threadIdx.x; k <= H; k += NT) tw[k] = twid[k];
-    const bool f = flip[img] != 0;
-    const float4* src = reinterpret_cast<const float4*>(stack + s * (int64_t)NN);
-    auto load = [&](int p, int& a, int& b) -> float4 {
-        const int e = 4 * p;
-        a = e >> LOGN;
-        b = e & (N - 1);
-        float4 v = src[(a * N + (f ? N - 4 - b : b)) >> 2];
-        if (f) v = make_float4(v.w, v.z, v.y, v.x);
-        return v;
-    };
-    // background statistics (reference :277-281)
-    KSum sum, sq;
-    for (int p = threadIdx.x; p < NQ; p += NT) {
-        int a, b;
-        const float4 v = load(p, a, b);
-        const float vv[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const float bg = vv[j] * (1.0f - mask_ref(b + j, a, N));
-            sum.add(bg);
-            sq.add(bg * bg);
-        }
-    }
-    const double tot = block_sum_double<NT>((double)sum.value(), red);
-    const double tot2 = block_sum_double<NT>((double)sq.value(), red);
-    const double mean = tot / NN;
-    const float fmean = (float)mean;
-    const float inv = (float)(1.0 / sqrt(fmax(tot2 / NN - mean * mean, 0.0)));
-    // normalised storage-orientation rows as packed complex pairs
-    for (int p = threadIdx.x; p < NQ; p += NT) {
-        int a, b;
-        const float4 v = load(p, a, b);
-        float2* row = C + a * RS + (b >> 1);
-        row[0] = make_float2((v.x - fmean) * inv, (v.y - fmean) * inv);
-        row[1] = make_float2((v.z - fmean) * inv, (v.w - fmean) * inv);
-    }
-    __syncthreads();
-    // rows: length-H complex FFT, then the real split X[k], k = 0..H
-    fft_dif<NT>(C, LOGH, N, RS, 1, tw, LOGN, false);
-    {
-        float2 o0[PER], o1[PER];
-#pragma unroll
-        for (int u = 0; u < PER; ++u) {
-            const int t = threadIdx.x + u * NT;
-            if (t >= PAIRS) break;
-            const int r = t / (H / 2 + 1), k = t - r * (H / 2 + 1);
-            const float2* row = C + r * RS;
-            const float2 zk = row[bitrev(k & (H - 1), LOGH)];
-            const float2 zm = row[bitrev((H - k) & (H - 1), LOGH)];
-            // X[k] = (zk + conj zm)/2 - i w_k (zk - conj zm)/2,  w_k = exp(-2 pi i k / N)
-            const float2 e = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
-            const float2 d = make_float2(0.5f * (zk.x - zm.x), 0.5f * (zk.y + zm.y));
-            const float2 wd = cmul(tw[k], d);
-            o0[u] = make_float2(e.x + wd.y, e.y - wd.x);
-            // X[H-k] from the same pair: (zm + conj zk)/2 - i w_{H-k} (zm - conj zk)/2
-            const float2 e2 = make_float2(0.5f * (zm.x + zk.x), 0.5f * (zm.y - zk.y));
-            const float2 d2 = make_float2(0.5f * (zm.x - zk.x), 0.5f * (zm.y + zk.y));
-            const float2 wd2 = cmul(tw[H - k], d2);
-            o1[u] = make_float2(e2.x + wd2.y, e2.y - wd2.x);
-        }
-        __syncthreads();
-#pragma unroll
-        for (int u = 0; u < PER; ++u) {
-            const int t = threadIdx.x + u * NT;
-            if (t >= PAIRS) break;
-            const int r = t / (H / 2 + 1), k = t - r * (H / 2 + 1);
-            float2* row = C + r * RS;
-            row[k] = o0[u];
-            row[H - k] = o1[u];
-        }
-        __syncthreads();
-    }
-    // columns: length-N complex FFT (rows come out bit-reversed), multiply by G/N^2, inverse
-    fft_dif<NT>(C, LOGN, RS, 1, RS, tw, LOGN, true);
-    for (int e = threadIdx.x; e < N * RS; e += NT) {
-        const int i = e / RS, kc = e - i * RS;
-        const float g = gtab[bitrev(i, LOGN) * RS + kc];
-        C[e] = make_float2(C[e].x * g, C[e].y * g);
-    }
-    __syncthreads();
-    fft_dit_inv<NT>(C, LOGN, RS, 1, RS, tw, LOGN, true);
-    // rows: inverse real split Z[k] = (X[k] + conj X[H-k]) + i conj(w_k)(X[k] - conj X[H-k]),
-    // stored bit-reversed for the inverse DIT, then the length-H inverse FFT
-    {
-        float2 o0[PER], o1[PER];
-#pragma unroll
-        for (int u = 0; u < PER; ++u) {
-            const int t = threadIdx.x + u * NT;
-            if (t >= PAIRS) break;
-            const int r = t / (H / 2 + 1), k = t - r * (H / 2 + 1);
-            const float2* row = C + r * RS;
-            const float2 xk = row[k], xm = row[H - k];
-            const float2 e = make_float2(xk.x + xm.x, xk.y - xm.y);
-            const float2 d = make_float2(xk.x - xm.x, xk.y + xm.y);
-            const float2 wd = cmulc(d, tw[k]);
-            o0[u] = make_float2(e.x - wd.y, e.y + wd.x);
-            const float2 e2 = make_float2(xm.x + xk.x, xm.y - xk.y);
-            const float2 d2 = make_float2(xm.x - xk.x, xm.y + xk.y);
-            const float2 wd2 = cmulc(d2, tw[H - k]);
-            o1[u] = make_float2(e2.x - wd2.y, e2.y + wd2.x);
-        }
-        __syncthreads();
-#pragma unroll
-        for (int u = 0; u < PER; ++u) {
-            const int t = threadIdx.x + u * NT;
-            if (t >= PAIRS) break;
-            const int r = t / (H / 2 + 1), k = t - r * (H / 2 + 1);
-            float2* row = C + r * RS;
-            if (k < H) row[bitrev(k, LOGH)] = o0[u];
-            if (k > 0 && k < H) row[bitrev(H - k, LOGH)] = o1[u];
-        }
-        __syncthreads();
-    }
-    fft_dit_inv<NT>(C, LOGH, N, RS, 1, tw, LOGN, false);
-    for (int p = threadIdx.x; p < N * H; p += NT) {
-        const int a = p >> LOGH, j = p & (H - 1);
-        reinterpret_cast<float2*>(dst)[p] = C[a * RS + j];
     }
 }
 
@@ -616,6 +428,201 @@ __global__ void __launch_bounds__(NT) rotate_kernel(
     for (int r = r0; r < N; r += R, X += dX, Y += dY) out[r * N + c] = sample_at(s, N, P, X, Y);
 }
 
+// Compile-time box size (power-of-two N, 512 threads): the same computation as rotate_kernel
+// with every loop bound, row stride and tap offset a constant, the tap indices wrapped by a
+// mask, the -1 of the 4-tap window folded into the fixed-point origin and the prefilter
+// recursions unrolled.  Segment start sums use kInitTaps taps (N >= kInitTaps).
+// Row stride of the coefficient image in the compile-time kernels: >= N + 3 (halo) and = 1 mod 32,
+// so that the bank of tap (ix, iy) is (ix + iy) mod 32; a warp's 32 samples along a line whose
+// direction has components of one sign then meet at most about two to a bank.
+template <int N>
+__host__ __device__ constexpr int rot_stride() {
+    return ((N + 3 + 30) / 32) * 32 + 1;
+}
+
+template <int NT, int N, int AXIS>
+__device__ __forceinline__ void prefilter_fixed(float* s) {
+    constexpr int P = rot_stride<N>();
+    constexpr int NSEG = (NT / N < N / 16) ? NT / N : N / 16;
+    constexpr int SEG = N / NSEG, LINES = N * NSEG;
+    constexpr int SK = AXIS == 0 ? 1 : P, SL = AXIS == 0 ? P : 1;
+    const int t = threadIdx.x;
+    const bool active = t < LINES;
+    const int line = t % N, g = t / N;
+    const int k0 = g * SEG, k1 = k0 + SEG - 1;
+    float* base = s + line * SL;
+    float init = 0.f;
+    if (active) {
+        float acc = 0.f, zp = 1.f;
+        if (k0 < kInitTaps - 1) {            // the taps wrap around the line's start
+#pragma unroll
+            for (int j = 0; j < kInitTaps; ++j) {
+                acc += zp * base[((k0 - j) & (N - 1)) * SK];
+                zp *= kZ1;
+            }
+        } else {
+            const float* b0 = base + k0 * SK;
+#pragma unroll
+            for (int j = 0; j < kInitTaps; ++j) {
+                acc += zp * b0[-j * SK];
+                zp *= kZ1;
+            }
+        }
+        init = acc;
+    }
+    __syncthreads();
+    if (active) {
+        float* b0 = base + k0 * SK;
+        float prev = init;
+        b0[0] = prev;
+#pragma unroll
+        for (int k = 1; k < SEG; ++k) {
+            prev = b0[k * SK] + kZ1 * prev;
+            b0[k * SK] = prev;
+        }
+    }
+    __syncthreads();
+    if (active) {
+        float acc = 0.f, zp = 1.f;
+        if (k1 + kInitTaps - 1 >= N) {       // the taps wrap around the line's end
+#pragma unroll
+            for (int j = 0; j < kInitTaps; ++j) {
+                acc += zp * base[((k1 + j) & (N - 1)) * SK];
+                zp *= kZ1;
+            }
+        } else {
+            const float* b1 = base + k1 * SK;
+#pragma unroll
+            for (int j = 0; j < kInitTaps; ++j) {
+                acc += zp * b1[j * SK];
+                zp *= kZ1;
+            }
+        }
+        init = acc;
+    }
+    __syncthreads();
+    if (active) {
+        constexpr float gain = -6.0f * kZ1;
+        float* b0 = base + k0 * SK;
+        float prev = init;
+        b0[(SEG - 1) * SK] = gain * prev;
+#pragma unroll
+        for (int k = SEG - 2; k >= 0; --k) {
+            prev = b0[k * SK] + kZ1 * prev;
+            b0[k * SK] = gain * prev;
+        }
+    }
+    __syncthreads();
+}
+
+// Two output samples a, b at once with paired FP32 instructions (fma.rn.f32x2 and friends);
+// per sample the same operations in the same order as bspline_w / sample_fixed.
+__device__ __forceinline__ void bspline_w2(float2 t, float2 w[4]) {
+    const float2 one = make_float2(1.f, 1.f), sixth = make_float2(1.f / 6.f, 1.f / 6.f);
+    const float2 two3 = make_float2(2.f / 3.f, 2.f / 3.f), half = make_float2(0.5f, 0.5f);
+    const float2 mone = make_float2(-1.f, -1.f);
+    const float2 u = __ffma2_rn(t, mone, one);
+    const float2 t2 = __fmul2_rn(t, t), u2 = __fmul2_rn(u, u);
+    w[0] = __fmul2_rn(__fmul2_rn(sixth, u2), u);
+    w[3] = __fmul2_rn(__fmul2_rn(sixth, t2), t);
+    // 2/3 - t^2 (1 - t/2) = 2/3 + t^2 (t/2 - 1)
+    w[1] = __ffma2_rn(t2, __ffma2_rn(half, t, mone), two3);
+    w[2] = __ffma2_rn(u2, __ffma2_rn(half, u, mone), two3);
+}
+
+template <int N>
+__device__ __forceinline__ float2 sample_fixed2(const float* s, int64_t XA, int64_t YA, int64_t XB,
+                                                int64_t YB) {
+    constexpr int P = rot_stride<N>();
+    const float2 k32 = make_float2(2.3283064365386963e-10f, 2.3283064365386963e-10f);
+    const float2 tx = __fmul2_rn(make_float2((float)(uint32_t)(XA & 0xffffffffll),
+                                             (float)(uint32_t)(XB & 0xffffffffll)), k32);
+    const float2 ty = __fmul2_rn(make_float2((float)(uint32_t)(YA & 0xffffffffll),
+                                             (float)(uint32_t)(YB & 0xffffffffll)), k32);
+    float2 wx[4], wy[4];
+    bspline_w2(tx, wx);
+    bspline_w2(ty, wy);
+    const float* a = s + ((int)(XA >> 32) & (N - 1)) * P + ((int)(YA >> 32) & (N - 1));
+    const float* b = s + ((int)(XB >> 32) & (N - 1)) * P + ((int)(YB >> 32) & (N - 1));
+    float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        float2 v = __fmul2_rn(wy[0], make_float2(a[i * P], b[i * P]));
+        v = __ffma2_rn(wy[1], make_float2(a[i * P + 1], b[i * P + 1]), v);
+        v = __ffma2_rn(wy[2], make_float2(a[i * P + 2], b[i * P + 2]), v);
+        v = __ffma2_rn(wy[3], make_float2(a[i * P + 3], b[i * P + 3]), v);
+        acc = __ffma2_rn(wx[i], v, acc);
+    }
+    return acc;
+}
+
+// One rotation of the coefficient image in smem into keep[]: thread t has u = t % N and
+// v0 = t / N; it samples output (r, c) = (v0 + k R, u) when the lanes run along output rows
+// (lane step (sin, cos) in (x, y)), or (u, v0 + k R) when they run along output columns (lane
+// step (cos, -sin)) -- whichever step has components of one sign.  Returns the smem index of
+// keep[0] and the stride of keep[k] in the [r][c] layout.
+template <int NT, int N>
+__device__ __forceinline__ void rotate_once(const float* s, const RotConst& Q, float* keep,
+                                            int& base, int& stride) {
+    constexpr int P = rot_stride<N>(), R = NT / N, MAXV = N / R;
+    constexpr int64_t kOne = 1ll << 32;
+    const int u = threadIdx.x % N, v0 = threadIdx.x / N;
+    const bool along_cols = (Q.rc > 0) != (Q.rs > 0);
+    const int r = along_cols ? u : v0, c = along_cols ? v0 : u;
+    int64_t X = Q.bx - kOne + (int64_t)r * Q.rc + (int64_t)c * Q.rs;
+    int64_t Y = Q.by - kOne - (int64_t)r * Q.rs + (int64_t)c * Q.rc;
+    const int64_t dX = (int64_t)R * (along_cols ? Q.rs : Q.rc);
+    const int64_t dY = (int64_t)R * (along_cols ? Q.rc : -Q.rs);
+#pragma unroll
+    for (int k = 0; k < MAXV; k += 2) {
+        const float2 v = sample_fixed2<N>(s, X, Y, X + dX, Y + dY);
+        keep[k] = v.x;
+        keep[k + 1] = v.y;
+        X += 2 * dX;
+        Y += 2 * dY;
+    }
+    base = r * P + c;
+    stride = along_cols ? R : R * P;
+}
+
+template <int NT, int N>
+__global__ void __launch_bounds__(NT, 2) rotate_fixed_kernel(
+        float* __restrict__ xbuf, float* __restrict__ img_out, const double* __restrict__ psi_rad,
+        const PdDev* __restrict__ pds, const int32_t* __restrict__ img_pd) {
+    constexpr int P = rot_stride<N>(), NN = N * N, R = NT / N, MAXV = N / R;
+    extern __shared__ float s[];
+    __shared__ RotConst rot[2];
+    const int64_t img = blockIdx.x;
+    float* xi = xbuf + img * (int64_t)NN;
+    if (threadIdx.x == 0) {
+        const double ang = -(180.0 / 3.141592653589793) * psi_rad[img];
+        const double t = ang * (3.141592653589793 / 180.0);
+        rot[0] = make_rot(cos(t), sin(t), N);
+        const PdDev& pd = pds[img_pd[img]];
+        rot[1] = make_rot(pd.rot2_cos, pd.rot2_sin, N);
+    }
+    for (int p = threadIdx.x; p < NN; p += NT) {
+        const int a = p / N, b = p % N;
+        s[b * P + a] = xi[p] * mask_ref(b, a, N);
+    }
+    __syncthreads();
+    float keep[MAXV];
+#pragma unroll 1
+    for (int pass = 0; pass < 2; ++pass) {
+        prefilter_fixed<NT, N, 0>(s);
+        prefilter_fixed<NT, N, 1>(s);
+        fill_halo<NT>(s, N, P);
+        int base, stride;
+        rotate_once<NT, N>(s, rot[pass], keep, base, stride);
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < MAXV; ++k) s[base + k * stride] = keep[k];
+        __syncthreads();
+    }
+    float* out = img_out + img * (int64_t)NN;
+    for (int p = threadIdx.x; p < NN; p += NT) out[p] = s[(p / N) * P + p % N];
+}
+
 // Boxes too large for the shared-memory kernel (N > 236): the same two rotations with the spline
 // coefficients in global memory (the image's own workspace slots, L1/L2-resident while the CTA
 // works on them).  A = the image's spectrum slot (free at this point, >= N*N floats), B = its
@@ -739,6 +746,7 @@ __global__ void __launch_bounds__(256) pd_sums_kernel(
         const int fa = min(ka, N - ka);
         const int m = fa * fa + kb * kb;
         KSum s0, s1, s2, s3, s4, s5;
+#pragma unroll 4
         for (int64_t i = it.img_begin; i < it.img_end; ++i) {
             const float2 F = spec[i * Kc + k];
             int sg;
@@ -809,7 +817,8 @@ __global__ void __launch_bounds__(256) pd_finalize_kernel(
 //     a_i  = sum_k (mu_u v_ik + mu_v u_ik - mu_u mu_v - mu_r r_ik + mu_r^2/2 - mu_s s_ik + mu_s^2/2)
 //   (an exact rewrite of D_ij = sum_k |C_j F_i - C_i F_j|^2 for any centring vector mu).
 //   Features are written scaled by the PD's power of two; a_i in FP64 unscaled.
-//   The spectrum is overwritten with sign(C) F / N^2 (input of the phase-flip inverse FFT).
+//   With write_signed the spectrum is overwritten with sign(C) F / N^2 (input of a cuFFT
+//   phase-flip C2R); the shared-memory inverse FFT applies sign(C) / N^2 itself.
 // ------------------------------------------------------------------------------------------
 // MODE 0: FP32 features; 1: bf16 hi/lo.  Frequency slot k (k >= Kc: zero padding) goes to
 // feature column colmap[k]: 64-wide chunks ordered so the dominant low frequencies are
@@ -823,7 +832,7 @@ __global__ void __launch_bounds__(256) features_kernel(
         const uint32_t* __restrict__ scale_bits, void* __restrict__ feat_a, void* __restrict__ feat_b,
         double* __restrict__ pair_norm, float* __restrict__ ctf_out,
         float2* __restrict__ spectrum_out, int N, int Nh, int64_t Kc, int64_t Kc_pad,
-        int64_t mstride, CtfConst cc) {
+        int64_t mstride, CtfConst cc, int write_signed) {
     __shared__ double red[32];
     const int64_t img = blockIdx.x;
     const int pd = img_pd[img];
@@ -835,6 +844,7 @@ __global__ void __launch_bounds__(256) features_kernel(
     const int64_t K4 = 4 * Kc_pad;
     float2* sp = spec + img * Kc;
     KSum acc;
+#pragma unroll 2
     for (int64_t k = threadIdx.x; k < Kc_pad; k += 256) {
         float fu = 0.f, fv = 0.f, fr = 0.f, fs = 0.f;
         const int64_t col = colmap[k];
@@ -861,8 +871,10 @@ __global__ void __launch_bounds__(256) features_kernel(
             fv = (v - mu_v) * sc;
             fr = (r - mu_r) * sc;
             fs = (s - mu_s) * sc;
-            const float sgf = (float)sg * inv_nn;
-            sp[k] = make_float2(sgf * F.x, sgf * F.y);
+            if (write_signed) {
+                const float sgf = (float)sg * inv_nn;
+                sp[k] = make_float2(sgf * F.x, sgf * F.y);
+            }
         }
         const float vals[4] = {fu, fv, fr, fs};
         if (MODE == 1) {
@@ -927,50 +939,25 @@ namespace mem {
 namespace kern {
 
 int gather_normalize(const mem_plan& P, const mem_inputs& in, float* xbuf, uint32_t* status,
-                     cudaStream_t s) {
+                     int64_t max_ctas, cudaStream_t s) {
     if (P.n_images == 0) return MEM_OK;
+    const int64_t grid = max_ctas > 0 ? std::min<int64_t>(max_ctas, P.n_images) : P.n_images;
     if (P.N % 4 == 0)
-        gather_normalize_v4_kernel<256><<<(unsigned)P.n_images, 256, 0, s>>>(
-            in.stack, in.num_stack, in.stack_index, in.flip, xbuf, P.N, status);
+        gather_normalize_v4_kernel<256><<<(unsigned)grid, 256, 0, s>>>(
+            in.stack, in.num_stack, in.stack_index, in.flip, xbuf, P.N, status, P.n_images);
     else
-        gather_normalize_kernel<256><<<(unsigned)P.n_images, 256, 0, s>>>(
-            in.stack, in.num_stack, in.stack_index, in.flip, xbuf, P.N, status);
+        gather_normalize_kernel<256><<<(unsigned)grid, 256, 0, s>>>(
+            in.stack, in.num_stack, in.stack_index, in.flip, xbuf, P.N, status, P.n_images);
     MEM_LAUNCH_CHECK();
     return MEM_OK;
 }
 
 int lowpass(const mem_plan& P, float2* spec, float* gtab, cudaStream_t s) {
     const int KcN = P.N * P.Nh;
-    lowpass_table_kernel<<<(KcN + 255) / 256, 256, 0, s>>>(
-        gtab, P.N, P.Nh, P.params.filter_type, P.params.filter_Qc, P.params.filter_order);
-    MEM_LAUNCH_CHECK();
     const int64_t total = P.n_images * (int64_t)KcN;
     if (total == 0) return MEM_OK;
     const int64_t blocks = std::min<int64_t>((total + 255) / 256, (int64_t)P.num_sms * 16);
     lowpass_apply_kernel<<<(unsigned)blocks, 256, 0, s>>>(spec, gtab, total, KcN);
-    MEM_LAUNCH_CHECK();
-    return MEM_OK;
-}
-
-bool lowpass_fused_supported(const mem_plan& P) {
-    const int N = P.N;
-    return N >= 16 && N <= 128 && (N & (N - 1)) == 0;
-}
-
-int lowpass_fused(const mem_plan& P, const mem_inputs& in, const float* gtab,
-                  const float2* twid, float* xbuf, uint32_t* status, cudaStream_t s) {
-    if (P.n_images == 0) return MEM_OK;
-    constexpr int NT = 512;
-    const size_t smem = (size_t)P.N * (P.N / 2 + 1) * sizeof(float2);
-#define MEM_LPF(LOGN)                                                                              do {                                                                                               MEM_CUDA_TRY(cudaFuncSetAttribute(lowpass_fused_kernel<NT, LOGN>,                                                                cudaFuncAttributeMaxDynamicSharedMemorySize,                                                   (int)smem));                                                 lowpass_fused_kernel<NT, LOGN><<<(unsigned)P.n_images, NT, smem, s>>>(                             in.stack, in.num_stack, in.stack_index, in.flip, gtab, twid, xbuf, status);            } while (0)
-    switch (P.N) {
-        case 16: MEM_LPF(4); break;
-        case 32: MEM_LPF(5); break;
-        case 64: MEM_LPF(6); break;
-        case 128: MEM_LPF(7); break;
-        default: return MEM_ERR_UNSUPPORTED;
-    }
-#undef MEM_LPF
     MEM_LAUNCH_CHECK();
     return MEM_OK;
 }
@@ -999,6 +986,16 @@ int rotate(const mem_plan& P, const mem_inputs& in, float* xbuf, float* img_out,
     const int Pst = ((N + 3) % 2 == 0) ? N + 4 : N + 3;     // odd row stride, 3-px halo
     const size_t smem = (size_t)(N + 3) * Pst * sizeof(float);
     constexpr int NT = 512;
+    if (N == 128 || N == 64) {
+        auto kfn = N == 128 ? rotate_fixed_kernel<NT, 128> : rotate_fixed_kernel<NT, 64>;
+        const size_t smem_f = (size_t)(N + 3) *
+                              (N == 128 ? rot_stride<128>() : rot_stride<64>()) * sizeof(float);
+        MEM_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem_f));
+        kfn<<<(unsigned)P.n_images, NT, smem_f, s>>>(xbuf, img_out, in.psi_rad, pd_table, img_pd);
+        MEM_LAUNCH_CHECK();
+        return MEM_OK;
+    }
     int nseg = std::max(1, std::min(NT / N, N / 16));
     const bool exact = N < kInitTaps;
     if (exact) nseg = 1;
@@ -1052,12 +1049,14 @@ int pd_finalize(const mem_plan& P, const float* partial, const SumItem* items,
 int features(const mem_plan& P, float2* spec, const uint64_t* qf, const PdDev* pds,
              const int32_t* img_pd, const int32_t* img_row, const int32_t* colmap,
              const float* means, const uint32_t* scale_bits, void* feat_a, void* feat_b,
-             double* pair_norm, float* ctf_out, float* spectrum_out, cudaStream_t s) {
+             double* pair_norm, float* ctf_out, float* spectrum_out, bool write_signed,
+             cudaStream_t s) {
     if (P.n_images == 0) return MEM_OK;
 #define MEM_FEATS(MODE)                                                                        \
     features_kernel<MODE><<<(unsigned)P.n_images, 256, 0, s>>>(                                \
         spec, qf, pds, img_pd, img_row, colmap, means, scale_bits, feat_a, feat_b, pair_norm,  \
-        ctf_out, (float2*)spectrum_out, P.N, P.Nh, P.Kc, P.Kc_pad, means_stride(P), P.ctf)
+        ctf_out, (float2*)spectrum_out, P.N, P.Nh, P.Kc, P.Kc_pad, means_stride(P), P.ctf,     \
+        write_signed ? 1 : 0)
     if (P.params.precision == MEM_PREC_SPLIT_BF16)
         MEM_FEATS(1);
     else

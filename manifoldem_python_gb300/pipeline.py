@@ -127,6 +127,20 @@ class Plan:
                                              ctypes.c_void_p(stream.cuda_stream)),
                    'mem_plan_execute')
 
+    def execute_split(self, stack, stack_index, flip, psi_rad, df, outputs: Dict[str, object],
+                      load_stream, stream) -> None:
+        """``execute`` with the stack-reading kernel on ``load_stream`` and the rest on
+        ``stream`` (mem_plan_execute_split); ``stack`` may be a pinned host tensor."""
+        cin = _lib.MemInputs(stack=stack.data_ptr(), num_stack=int(stack.shape[0]),
+                             stack_index=stack_index.data_ptr(), flip=flip.data_ptr(),
+                             psi_rad=psi_rad.data_ptr(), df=df.data_ptr())
+        cout = _lib.MemOutputs(**{k: _ptr(outputs.get(k)) for k in OUTPUT_NAMES})
+        self._keep = (cin, cout)
+        _lib.check(self.lib.mem_plan_execute_split(
+            self.handle, ctypes.byref(cin), ctypes.byref(cout), self.workspace.data_ptr(),
+            self.ws_bytes, ctypes.c_void_p(load_stream.cuda_stream),
+            ctypes.c_void_p(stream.cuda_stream)), 'mem_plan_execute_split')
+
     def capture(self, stack, stack_index, flip, psi_rad, df, outputs: Dict[str, object]):
         """Capture one execute (every kernel and cuFFT launch of the stage) in a CUDA graph and
         return it; ``graph.replay()`` reruns the stage on the same buffers.  Input and output
@@ -228,6 +242,103 @@ class DistanceStage:
         torch.cuda.synchronize(dev)
         plan.device_status()
         return split_outputs(plan, counts, outs, to_host)
+
+
+def balanced_groups(counts: Sequence[int], n_groups: int) -> List[range]:
+    """Consecutive PD ranges with about equal image counts (at most n_groups, none empty)."""
+    counts = np.asarray(counts, dtype=np.int64)
+    n_groups = max(1, min(int(n_groups), len(counts)))
+    cum = np.cumsum(counts)
+    cuts = [0]
+    for g in range(1, n_groups):
+        c = int(np.searchsorted(cum, cum[-1] * g / n_groups, side='left')) + 1
+        cuts.append(min(max(c, cuts[-1] + 1), len(counts) - (n_groups - g)))
+    cuts.append(len(counts))
+    return [range(a, b) for a, b in zip(cuts[:-1], cuts[1:])]
+
+
+class StreamedStage:
+    """The stage for many PDs with the image stack left in pinned host memory.
+
+    The PDs are split into ``n_groups`` consecutive groups of about equal image count, one plan
+    each.  Every ``run`` issues, per group, the per-image metadata copy and the stack-reading
+    kernel on a high-priority load stream (a small grid reading the images over the host link,
+    ``mem_plan_execute_split``), the rest of the stage on a compute stream, and the copy of the
+    results into pinned host buffers on a copy stream.  Group g+1's images arrive while group g
+    computes, and group g's results leave while group g+1 computes.
+    """
+
+    def __init__(self, params: StageParams, counts: Sequence[int], psi_p: Sequence[float],
+                 n_groups: int = 4, outputs=('D', 'img_avg', 'img_avg_flip', 'img_all_intensity'),
+                 device=None):
+        import torch
+        self.device = torch.device(device or 'cuda')
+        self.counts = [int(c) for c in counts]
+        self.groups = balanced_groups(self.counts, n_groups)
+        psi_p = np.asarray(psi_p, dtype=np.float64)
+        self.plans = [Plan(params, [self.counts[i] for i in g], psi_p[list(g)], self.device)
+                      for g in self.groups]
+        self.outputs = outputs
+        self.dev_out = [p.allocate_outputs(outputs) for p in self.plans]
+        self.host_out = [{k: torch.empty(v.shape, dtype=v.dtype, pin_memory=True)
+                          for k, v in d.items()} for d in self.dev_out]
+        lo, hi = torch.cuda.Stream.priority_range() if hasattr(torch.cuda.Stream,
+                                                                 'priority_range') else (0, -1)
+        self.load_stream = torch.cuda.Stream(self.device, priority=min(lo, hi))
+        self.stream = torch.cuda.Stream(self.device)
+        self.copy_stream = torch.cuda.Stream(self.device)
+        img_off = np.concatenate([[0], np.cumsum(self.counts)])
+        self.img_ranges = [(int(img_off[g.start]), int(img_off[g.stop])) for g in self.groups]
+        self._meta_h = None
+
+    def set_metadata(self, stack_index, flip, psi_rad, df) -> None:
+        """Per-image inputs over all PDs in plan order (host arrays); copied per run."""
+        import torch
+        arrays = [np.ascontiguousarray(stack_index, dtype=np.int64),
+                  np.ascontiguousarray(flip, dtype=np.uint8),
+                  np.ascontiguousarray(psi_rad, dtype=np.float64),
+                  np.ascontiguousarray(df, dtype=np.float64)]
+        self._meta_h, self._meta_d = [], []
+        for a, b in self.img_ranges:
+            hs = [torch.from_numpy(x[a:b].copy()).pin_memory() for x in arrays]
+            self._meta_h.append(hs)
+            self._meta_d.append([torch.empty_like(h, device=self.device) for h in hs])
+
+    def metadata_bytes(self) -> int:
+        return sum(t.numel() * t.element_size() for hs in self._meta_h for t in hs)
+
+    def result_bytes(self) -> int:
+        return sum(t.numel() * t.element_size() for d in self.host_out for t in d.values())
+
+    def run(self, stack):
+        """One pass over all PDs; ``stack`` is a pinned host (or device) tensor.  Returns the
+        per-group pinned host outputs (valid until the next run)."""
+        import torch
+        if self._meta_h is None:
+            raise RuntimeError('set_metadata first')
+        cur = torch.cuda.current_stream(self.device)
+        for s in (self.load_stream, self.stream, self.copy_stream):
+            s.wait_stream(cur)
+        for g, plan in enumerate(self.plans):
+            with torch.cuda.stream(self.load_stream):
+                for dst, src in zip(self._meta_d[g], self._meta_h[g]):
+                    dst.copy_(src, non_blocking=True)
+            sidx, flip, psi, df = self._meta_d[g]
+            plan.execute_split(stack, sidx, flip, psi, df, self.dev_out[g], self.load_stream,
+                               self.stream)
+            done = torch.cuda.Event()
+            done.record(self.stream)
+            self.copy_stream.wait_event(done)
+            with torch.cuda.stream(self.copy_stream):
+                for k, v in self.dev_out[g].items():
+                    self.host_out[g][k].copy_(v, non_blocking=True)
+        self.copy_stream.synchronize()
+        self.stream.synchronize()
+        return self.host_out
+
+    def device_status(self) -> None:
+        for p in self.plans:
+            p.device_status()
 
 
 def split_outputs(plan: Plan, counts: Sequence[int], outs: Dict[str, object], to_host: bool):

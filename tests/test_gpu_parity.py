@@ -141,10 +141,11 @@ def test_dropin_op_writes_reference_pickle(cuda_ready):
     assert d['options'] == options
 
 
-@pytest.mark.parametrize('N', [192, 250])
-def test_large_boxes_match_oracle(cuda_ready, N):
-    """Boxes beyond the shared-memory rotation (250 px) and the 192 px workload size, against
-    the FP64 oracle on a small PD with conjugate views."""
+@pytest.mark.parametrize('N', [64, 128, 192, 250])
+def test_box_sizes_match_oracle(cuda_ready, N):
+    """Box sizes with their own kernels, against the FP64 oracle on a small PD with conjugate
+    views: 64 and 128 px (shared-memory FFTs, compile-time-size rotation), the 192 px workload
+    size (cuFFT) and 250 px (rotation with global-memory coefficients)."""
     torch = cuda_ready
     import dataclasses
     from manifoldem_python_gb300.pipeline import DistanceStage, PdJob, StageParams
@@ -162,3 +163,41 @@ def test_large_boxes_match_oracle(cuda_ready, N):
         assert rel(res['img_all_flip'], ref['imgAllFlip']) < TOL_IMG
         assert rel(res['img_avg'], ref['imgAvg']) < TOL_IMG
         assert rel(res['D'], ref['D']) < 1e-5
+
+
+def test_streamed_stage_matches_plain(cuda_ready):
+    """StreamedStage (stack in pinned host memory, PD groups on load / compute / copy streams,
+    mem_plan_execute_split) against one plain execute with the stack on the device."""
+    torch = cuda_ready
+    import dataclasses
+    from manifoldem_python_gb300.geometry import pd_geometry
+    from manifoldem_python_gb300.pipeline import (DistanceStage, PdJob, StageParams,
+                                                  StreamedStage, split_outputs)
+    from manifoldem_python_gb300.synthetic import CONFIGS, make_dataset
+    for N in (48, 64):
+        cfg = dataclasses.replace(CONFIGS['config4'], N=N, n_pd=7, n_median=60, n_min=1,
+                                  n_max=150, seed=70 + N)
+        ds = make_dataset(cfg, device='cpu')
+        params = StageParams(N=N, pix_size=cfg.pix, Cs=cfg.cs, EkV=cfg.kv, AmpContrast=cfg.ampc,
+                             precision='bf16x3')
+        jobs = [PdJob(ind=ind, q=ds.q[:, ind], df=ds.df[ind]) for ind in ds.CG]
+        names = ('D', 'img_avg', 'img_avg_flip', 'img_all_intensity')
+        ref = DistanceStage(params).run(jobs, ds.stack.cuda(), ds.nStot, outputs=names)
+        geoms = [pd_geometry(np.asarray(j.ind), j.q, ds.nStot) for j in jobs]
+        counts = [len(j.ind) for j in jobs]
+        st = StreamedStage(params, counts, [g.psi_p for g in geoms], n_groups=3, outputs=names)
+        st.set_metadata(np.concatenate([g.stack_index for g in geoms]),
+                        np.concatenate([g.flip for g in geoms]),
+                        np.concatenate([g.psi_rad for g in geoms]),
+                        np.concatenate([np.asarray(j.df, np.float64) for j in jobs]))
+        stack_h = ds.stack.contiguous().pin_memory()
+        for _ in range(2):                      # two runs in a row reuse every buffer
+            host = st.run(stack_h)
+        st.device_status()
+        got = []
+        for gi, (g, plan) in enumerate(zip(st.groups, st.plans)):
+            got += split_outputs(plan, [counts[i] for i in g], host[gi], to_host=True)
+        assert len(got) == len(ref)
+        for a, b in zip(got, ref):
+            for k in names:
+                np.testing.assert_array_equal(np.asarray(a[k]), np.asarray(b[k]))

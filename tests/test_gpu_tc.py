@@ -112,25 +112,30 @@ def test_tc_accumulation_groups(cuda_ready, group, kahan, terms):
 
 
 @pytest.mark.parametrize('N', [32, 64, 128])
-def test_fused_lowpass_matches_cufft_path(cuda_ready, N):
-    """The shared-memory FFT low-pass (power-of-two N) against the cuFFT path, same inputs."""
+def test_smem_fft_matches_cufft_path(cuda_ready, N):
+    """The shared-memory FFT kernels (low-pass, spectrum, inverse) against the cuFFT path on the
+    same inputs: every output of the stage."""
     torch = cuda_ready
+    from manifoldem_python_gb300.pipeline import DistanceStage, PdJob, StageParams
     cfg, ds = _dataset(N, 40, conj=0.5, seed=44 + N)
+    names = ('D', 'img_all', 'img_all_flip', 'img_avg', 'img_avg_flip', 'img_all_intensity',
+             'spectrum', 'ctf')
     outs = {}
-    for fused in (0, 1):
-        from manifoldem_python_gb300.pipeline import DistanceStage, PdJob, StageParams
-        old = os.environ.get('MEM_FUSED_LOWPASS')
-        os.environ['MEM_FUSED_LOWPASS'] = str(fused)
+    for smem in (0, 1):
+        old = os.environ.get('MEM_SMEM_FFT')
+        os.environ['MEM_SMEM_FFT'] = str(smem)
         try:
             st = DistanceStage(StageParams(N=cfg.N, pix_size=cfg.pix, Cs=cfg.cs, EkV=cfg.kv,
                                            AmpContrast=cfg.ampc))
             ind = ds.CG[0]
-            outs[fused] = st.run([PdJob(ind=ind, q=ds.q[:, ind], df=ds.df[ind])],
-                                 ds.stack.to('cuda'), ds.nStot, outputs=('D', 'img_all'))[0]
+            outs[smem] = st.run([PdJob(ind=ind, q=ds.q[:, ind], df=ds.df[ind])],
+                                ds.stack.to('cuda'), ds.nStot, outputs=names)[0]
         finally:
             if old is None:
-                os.environ.pop('MEM_FUSED_LOWPASS', None)
+                os.environ.pop('MEM_SMEM_FFT', None)
             else:
-                os.environ['MEM_FUSED_LOWPASS'] = old
-    assert rel(outs[1]['img_all'], outs[0]['img_all']) < 2e-6
-    assert rel(outs[1]['D'], outs[0]['D']) < 2e-6
+                os.environ['MEM_SMEM_FFT'] = old
+    for k in names:
+        e = rel(np.asarray(outs[1][k]), np.asarray(outs[0][k]))
+        print('N=%d %s: smem FFT vs cuFFT %.3g' % (N, k, e))
+        assert e < 2e-6, (k, e)

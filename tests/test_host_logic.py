@@ -67,3 +67,20 @@ def test_params_module_prefers_loaded_reference_p():
     finally:
         del sys.modules['p']
     assert params_module() is mp
+
+
+def test_balanced_groups_cover_pds_in_order():
+    """StreamedStage's PD groups: consecutive, non-empty, covering every PD once, image counts
+    close to equal."""
+    import numpy as np
+    from manifoldem_python_gb300.pipeline import balanced_groups
+    rng = np.random.default_rng(3)
+    for n_pd, n_groups in ((800, 4), (5, 3), (1, 4), (8, 8), (37, 6)):
+        counts = rng.integers(1, 900, n_pd)
+        groups = balanced_groups(counts, n_groups)
+        assert len(groups) == min(n_groups, n_pd)
+        assert [i for g in groups for i in g] == list(range(n_pd))
+        assert all(len(g) > 0 for g in groups)
+        if n_pd >= 100:
+            sizes = [int(counts[list(g)].sum()) for g in groups]
+            assert max(sizes) - min(sizes) <= 2 * counts.max()
