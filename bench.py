@@ -131,6 +131,54 @@ def cpu_sample_tasks(ds, pds, mic, sizes=None):
     return tasks
 
 
+def _oracle_dm(task):
+    """Worker: the FP64 restatement of DMembeddingII.op on one PD's D; (n, seconds, psi[:, :8])."""
+    D, seed = task
+    from oracle.dm_embedding import dm_embedding
+    t0 = time.perf_counter()
+    _, psi, _ = dm_embedding(D, seed=seed)
+    return D.shape[0], time.perf_counter() - t0, psi[:, :8]
+
+
+def dm_report(outs, counts, n_sample, cores):
+    """Diffusion-map embedding (the stage's consumer, DMembeddingII.op) of a sample of the
+    benchmark's own PDs: GPU op (manifoldem_python_gb300.DMembeddingII) wall time per PD
+    against the FP64 CPU port on the host cores, and the largest top-8 subspace angle."""
+    import multiprocessing as mp
+    import torch
+    from scipy.linalg import subspace_angles
+    from manifoldem_python_gb300 import DMembeddingII
+    cnt = np.asarray(counts)
+    order = np.argsort(cnt, kind='stable')
+    pick = sorted({int(order[int((q + 0.5) / n_sample * len(order))]) for q in range(n_sample)})
+    d_off = np.concatenate([[0], np.cumsum(cnt.astype(np.int64) ** 2)])
+    Ds = [outs['D'][d_off[p]:d_off[p + 1]].view(int(cnt[p]), int(cnt[p])) for p in pick]
+    DMembeddingII.op(Ds[0], Ds[0].shape[0], 3, 60000)            # warm-up (library load)
+    torch.cuda.synchronize()
+    gpu_psi, t_gpu = [], 0.0
+    for D in Ds:
+        np.random.seed(0)
+        t0 = time.perf_counter()
+        psi = DMembeddingII.op(D, D.shape[0], 3, 60000)[1]
+        t_gpu += time.perf_counter() - t0
+        gpu_psi.append(psi[:, :8])
+    host = [(D.cpu().numpy(), 0) for D in Ds]
+    os.environ.setdefault('OMP_NUM_THREADS', '1')
+    os.environ.setdefault('OPENBLAS_NUM_THREADS', '1')
+    t0 = time.perf_counter()
+    with mp.get_context('spawn').Pool(processes=min(cores, len(host))) as pool:
+        res = pool.map(_oracle_dm, host, chunksize=1)
+    cpu_wall = time.perf_counter() - t0
+    ang = max(float(np.max(subspace_angles(a, r[2]))) for a, r in zip(gpu_psi, res))
+    return dict(pds=len(Ds), n=[int(cnt[p]) for p in pick],
+                gpu_ms_per_pd=1e3 * t_gpu / len(Ds),
+                cpu_ms_per_pd_one_core=1e3 * float(np.mean([r[1] for r in res])),
+                cpu_cores=min(cores, len(host)), cpu_wall_s=cpu_wall,
+                max_top8_subspace_angle_rad=ang,
+                method='GPU: csrc/dmap.cu sweep + kernel, torch.linalg.eigh, host tanh fit; '
+                       'CPU: FP64 port of DMembeddingII/fergusonE/slaplacianonFly (oracle/)')
+
+
 def run_cpu_tasks(tasks, cores):
     import multiprocessing as mp
     os.environ.setdefault('OMP_NUM_THREADS', '1')
@@ -297,6 +345,10 @@ def run_gpu(args, rank, world):
     lib.mem_plan_set_timing(plan.handle, 0)
     phases = {lib.mem_phase_name(i).decode(): float(phase_ms[i]) for i in range(9)}
 
+    dm = None
+    if not args.no_dm and 'D' in outs and rank == 0:
+        dm = dm_report(outs, counts, args.dm_pds, os.cpu_count() or 1)
+
     # end to end through the public API with host buffers
     e2e = None
     n_pairs, n_images, graph_used = plan.n_pairs, plan.n_images, graph is not None
@@ -360,7 +412,7 @@ def run_gpu(args, rank, world):
         del stack_h
     return dict(ms=ms, pairs=n_pairs, n_images=n_images, counts=counts,
                 graph=graph_used, l2_flush=flush,
-                phases=phases, clocks=clk.summary(), t_gen=t_gen, e2e=e2e, ds=ds, cfg=cfg,
+                phases=phases, clocks=clk.summary(), t_gen=t_gen, e2e=e2e, ds=ds, cfg=cfg, dm=dm,
                 kernels=kernels_per_execute(outputs, False, cfg.N), outputs=outputs)
 
 
@@ -473,6 +525,9 @@ def main():
                          'load / compute / copy streams; copy: one host-to-device copy of the '
                          'stack, then one execute')
     ap.add_argument('--e2e-groups', type=int, default=4)
+    ap.add_argument('--no-dm', action='store_true',
+                    help='skip the diffusion-map embedding of a sample of PDs (GPU vs CPU port)')
+    ap.add_argument('--dm-pds', type=int, default=8)
     ap.add_argument('--no-precision', action='store_true',
                     help='skip the FP64 / diffusion-map precision report of one sample PD')
     ap.add_argument('--cpu-max-n', type=int, default=900)
@@ -571,6 +626,8 @@ def main():
         line['e2e'] = dict(value=pairs_total / (e['ms'] * 1e-3), unit='pairs/s',
                            h2d_bytes_per_step=e['h2d'], d2h_bytes_per_step=e['d2h'],
                            ms_per_step=e['ms'], pinned=e['pinned'], mode=e['mode'])
+    if r.get('dm'):
+        line['dm_embedding'] = r['dm']
     if not args.no_precision:
         line['precision'] = precision_report(args, r['ds'], r['counts'], cfg, args.precision)
     if not args.no_cpu_baseline:

@@ -187,6 +187,29 @@ int mem_pd_batch(const mem_params* params, int32_t n_pd, const int32_t* pd_count
 int mem_pd_distances_noalloc(const mem_params* params, int32_t n, const float* spectra,
                              const double* df, double* D, void* stream);
 
+/* ---- diffusion-map embedding of one PD's D (the stage's consumer) -----------------------
+ * The dense-matrix work of DMembeddingII.op (modules/DMembeddingII.py:86-185) with
+ * fergusonE.op (modules/fergusonE.py:33-58) and slaplacianonFly.op (:42-81), on device memory;
+ * the caller keeps the neighbour lists, the tanh fit and the eigen-decomposition (as the Python
+ * op in manifoldem_python_gb300/DMembeddingII.py does).
+ *
+ * mem_dm_symmetrise: Y (n x n f64) from D (n x n f64): the reference's symmetrised list of
+ *   squared distances (DMembeddingII.py:112-139): s_ij = sqrt(D_ji) when j is a listed neighbour
+ *   of point i (listed[i*n + j] != 0; listed == NULL lists every point, k = n), D_ji >= 1e-6 and
+ *   j != i, else 0; Y_ij = s_ij^2 + s_ji^2 - s_ij s_ji; entries that are not edges are -1.
+ * mem_dm_sweep: sums[e] = sum over edges (Y >= 0) of exp(-d), d = Y/(2 eps_e), over the terms
+ *   with d < thr (fergusonE.py:36-44); scale[e] = log2(e)/(2 eps_e) (device, float32, at most
+ *   2048 values).  exp in float32, sums in float64.
+ * mem_dm_laplacian: Y becomes the symmetric normalised kernel L of slaplacianonFly (alpha = 1):
+ *   W = exp(-Y/sigma^2) on edges, W'_ij = W_ij/(d_i d_j) (d = column sums of W),
+ *   L_ij = W'_ij/(e_i e_j) (e = sqrt(column sums of W')), L = |L + L^T|/2; scratch holds 2n
+ *   doubles.                                                                                */
+int mem_dm_symmetrise(const double* D, int64_t n, const uint8_t* listed, double* Y,
+                      void* stream);
+int mem_dm_sweep(const double* Y, int64_t n, const float* scale, int32_t n_eps, double thr,
+                 double* sums, void* stream);
+int mem_dm_laplacian(double* Y, int64_t n, double sigma, double* scratch, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -55,8 +55,12 @@ def count(N) -> int:
 
 def run_jobs(jobs: list, stack_file: str, nStot: int, options: dict, progress=None,
              budget_bytes: Optional[int] = None, precision: Optional[str] = None,
-             done_offset: int = 0, total: Optional[int] = None) -> None:
-    """Run ``jobs`` ([ind, q, df, outFile, prD] each) in HBM-admitted GPU batches."""
+             done_offset: int = 0, total: Optional[int] = None, writers: int = 4,
+             image_dtype=np.float64) -> None:
+    """Run ``jobs`` ([ind, q, df, outFile, prD] each) in HBM-admitted GPU batches; the pickles
+    and markers of a batch are written by ``writers`` threads while the next batch computes
+    (``writers=0``: written in line, as the reference does).  Progress is reported per PD when
+    its marker is queued."""
     import torch
 
     p = params_module()
@@ -69,27 +73,46 @@ def run_jobs(jobs: list, stack_file: str, nStot: int, options: dict, progress=No
     counts = [int(np.asarray(j[0]).shape[0]) for j in jobs]
     done = done_offset
     total = total or len(jobs)
-    for batch in admit_batches(counts, params, budget_bytes):
-        pj = [PdJob(ind=np.asarray(jobs[i][0]), q=np.asarray(jobs[i][1], dtype=np.float64),
-                    df=np.asarray(jobs[i][2], dtype=np.float64), outFile=jobs[i][3],
-                    prD=jobs[i][4]) for i in batch]
-        geoms = stage.geometry(pj, nStot)
-        all_idx = np.concatenate([g.stack_index for g in geoms])
-        imgs, compact = read_spider_images(stack_file, all_idx, N)
-        off = 0
-        for g in geoms:
-            g.stack_index = compact[off:off + g.stack_index.size]
-            off += g.stack_index.size
-        stack = torch.from_numpy(imgs).to(stage.device)
-        results = stage.run(pj, stack, nStot, outputs=DEFAULT_OUTPUTS, geoms=geoms)
-        for job, geom, res in zip(pj, geoms, results):
-            out = assemble(job, geom, res, N, options)
-            myio.fout1(job.outFile, OUTPUT_KEYS, [out[k] for k in OUTPUT_KEYS])
-            open(os.path.join(p.dist_prog, '%s' % job.prD), 'a').close()
-            done += 1
-            if progress is not None:
-                progress.emit(int((done / float(total)) * 100))
-        del stack, results
+    writer = myio.AsyncWriter(writers) if writers > 0 else None
+    try:
+        for batch in admit_batches(counts, params, budget_bytes):
+            done = _run_batch(stage, params, jobs, batch, stack_file, nStot, options, N, p,
+                              writer, image_dtype, progress, done, total)
+    finally:
+        if writer is not None:
+            writer.close()
+
+
+def _run_batch(stage, params, jobs, batch, stack_file, nStot, options, N, p, writer,
+               image_dtype, progress, done, total):
+    """One HBM-admitted batch: read its images, run the stage, queue its pickles."""
+    import torch
+    pj = [PdJob(ind=np.asarray(jobs[i][0]), q=np.asarray(jobs[i][1], dtype=np.float64),
+                df=np.asarray(jobs[i][2], dtype=np.float64), outFile=jobs[i][3],
+                prD=jobs[i][4]) for i in batch]
+    geoms = stage.geometry(pj, nStot)
+    all_idx = np.concatenate([g.stack_index for g in geoms])
+    imgs, compact = read_spider_images(stack_file, all_idx, N)
+    off = 0
+    for g in geoms:
+        g.stack_index = compact[off:off + g.stack_index.size]
+        off += g.stack_index.size
+    stack = torch.from_numpy(imgs).to(stage.device)
+    results = stage.run(pj, stack, nStot, outputs=DEFAULT_OUTPUTS, geoms=geoms)
+    for job, geom, res in zip(pj, geoms, results):
+        out = assemble(job, geom, res, N, options, image_dtype=image_dtype)
+        marker = os.path.join(p.dist_prog, '%s' % job.prD)
+        vals = [out[k] for k in OUTPUT_KEYS]
+        if writer is not None:
+            writer.submit(job.outFile, OUTPUT_KEYS, vals, marker)
+        else:
+            myio.fout1(job.outFile, OUTPUT_KEYS, vals)
+            open(marker, 'a').close()
+        done += 1
+        if progress is not None:
+            progress.emit(int((done / float(total)) * 100))
+    del stack, results
+    return done
 
 
 def op(*argv):

@@ -21,7 +21,8 @@ REPO = os.path.dirname(HERE)
 INCLUDE = os.path.join(REPO, 'include')
 BUILD_DIR = os.path.join(REPO, '_build')
 LIB_PATH = os.path.join(HERE, 'libmanifoldem_gb300.so')
-SOURCES = ['abi.cu', 'prologue.cu', 'gemm_fp32.cu', 'gemm_tc.cu', 'noalloc.cu', 'image_fft.cu']
+SOURCES = ['abi.cu', 'prologue.cu', 'gemm_fp32.cu', 'gemm_tc.cu', 'noalloc.cu', 'image_fft.cu',
+           'dmap.cu']
 ARCH_FLAGS = ['-gencode', 'arch=compute_103a,code=sm_103a']
 
 # status codes (include/manifoldem_gb300.h)
@@ -141,6 +142,10 @@ SIGNATURES = {
                                          ctypes.POINTER(MemOutputs), c_void_p, c_size_t, c_void_p,
                                          c_void_p]),
     'mem_workspace_status': (c_int32, [c_void_p, c_void_p]),
+    'mem_dm_symmetrise': (c_int32, [c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
+    'mem_dm_sweep': (c_int32, [c_void_p, c_int64, c_void_p, c_int32, c_double, c_void_p,
+                               c_void_p]),
+    'mem_dm_laplacian': (c_int32, [c_void_p, c_int64, c_double, c_void_p, c_void_p]),
     'mem_plan_set_timing': (c_int32, [c_void_p, c_int32]),
     'mem_plan_phase_times': (c_int32, [c_void_p, ctypes.POINTER(ctypes.c_float), c_int32]),
     'mem_phase_name': (ctypes.c_char_p, [c_int32]),

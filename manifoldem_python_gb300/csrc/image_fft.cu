@@ -241,20 +241,6 @@ struct Fft2 {
         }
     }
 
-    template <int K2>
-    static __device__ __forceinline__ void unpack_packed(const float2* v, int k1, int c,
-                                                         float2* __restrict__ spec) {
-        if constexpr (K2 < R2) {
-            const float2 m = mirror<K2>(v, k1);
-            if (c == 0) {
-                const int j = k1 + R1 * K2;
-                spec[j * HS] = make_float2(0.5f * (v[K2].x + m.x), 0.5f * (v[K2].y - m.y));
-                spec[j * HS + H] = make_float2(0.5f * (v[K2].y + m.y), 0.5f * (m.x - v[K2].x));
-            }
-            unpack_packed<K2 + 1>(v, k1, c, spec);
-        }
-    }
-
     // column pass 2 with the low-pass: forward DFT, multiply by G/N^2 (gtab [N][N/2+1];
     // G(j, .) = G(N-j, .)), inverse DFT
     static __device__ __forceinline__ void cols_filter(float2* S, const float2* W,
@@ -283,7 +269,39 @@ struct Fft2 {
         }
     }
 
-    // column pass 2 of the forward transform, written out as the half-plane spectrum
+    // Row-by-row access to the digit-reversed column spectra: thread t owns column c = t % H
+    // and rows j = j0 + 4 i (j0 = t / H < 4, i < N/4).  For those rows the digit-reversed
+    // position is R2 j0 + delta(i) with a compile-time delta, so the slot's pair-row, parity and
+    // most of its swizzle are constants of the unrolled loop.
+    static constexpr int kRowsPerThread = N / 4;
+    static_assert(NT == 4 * H && R1 % 4 == 0, "row walk: four row phases, R1 a multiple of 4");
+    static __device__ __forceinline__ int rdelta(int i) {
+        return 4 * R2 * (i % (R1 / 4)) + i / (R1 / 4);
+    }
+    // storage index of (column c, row j0 + 4 i); q0 = pos(c), q1 = pos of c's odd slot
+    static __device__ __forceinline__ int row_slot(int j0, int i, int q0, int q1) {
+        const int a = R2 * j0 + rdelta(i);
+        return addr(a >> 1, (rdelta(i) & 1) ? q1 : q0);
+    }
+
+    // the packed column's half-plane values from its spectrum Y (lanes of one column)
+    template <int K2>
+    static __device__ __forceinline__ void unpack_packed(const float2* v, int k1, int c,
+                                                         float2* __restrict__ spec) {
+        if constexpr (K2 < R2) {
+            const float2 m = mirror<K2>(v, k1);
+            if (c == 0) {
+                const int j = k1 + R1 * K2;
+                spec[j * HS] = make_float2(0.5f * (v[K2].x + m.x), 0.5f * (v[K2].y - m.y));
+                spec[j * HS + H] = make_float2(0.5f * (v[K2].y + m.y), 0.5f * (m.x - v[K2].x));
+            }
+            unpack_packed<K2 + 1>(v, k1, c, spec);
+        }
+    }
+
+    // column pass 2 of the forward transform, written out as the half-plane spectrum straight
+    // from registers (row segments of 32 bytes, merged in L2; measured faster than staging the
+    // rows through shared memory for coalesced stores)
     static __device__ __forceinline__ void cols_spectrum_out(const float2* S,
                                                              float2* __restrict__ spec) {
         const int w = warp(), l = lane();
@@ -301,8 +319,9 @@ struct Fft2 {
         }
     }
 
-    // inverse column pass 1 from a half-plane spectrum in global memory; SIGNED multiplies
-    // element (j, c) by sign(C(m)) / N^2, m = min(j, N-j)^2 + c^2 (the phase flip)
+    // inverse column pass 1 from a half-plane spectrum in global memory, read row by row
+    // (coalesced) into the columns' digit-reversed slots; SIGNED multiplies element (j, c) by
+    // sign(C(m)) / N^2, m = min(j, N-j)^2 + c^2 (the phase flip)
     template <bool SIGNED>
     static __device__ __forceinline__ float2 spec_at(const float2* __restrict__ spec, int j, int c,
                                                      uint64_t qf, const CtfConst& cc) {
@@ -317,24 +336,30 @@ struct Fft2 {
     static __device__ __forceinline__ void cols_spectrum_in(float2* S, const float2* W,
                                                             const float2* __restrict__ spec,
                                                             uint64_t qf, const CtfConst& cc) {
+        {
+            const int c = threadIdx.x % H, j0 = threadIdx.x / H;
+            const int q0 = pos(c), q1 = pos(c == 0 ? H : N - c);
+#pragma unroll 8
+            for (int i = 0; i < kRowsPerThread; ++i) {
+                const int j = j0 + 4 * i;
+                float2 y = spec_at<SIGNED>(spec, j, c, qf, cc);
+                if (c == 0) {                              // S0 + i S_{N/2}
+                    const float2 b = spec_at<SIGNED>(spec, j, H, qf, cc);
+                    y = make_float2(y.x - b.y, y.y + b.x);
+                }
+                S[row_slot(j0, i, q0, q1)] = y;
+            }
+        }
+        __syncthreads();
         const int w = warp(), l = lane();
 #pragma unroll
         for (int i = 0; i < IT2; ++i) {
             const int c = 8 * w + LP2 * i + l / R1, k1 = l % R1;
+            const int q0 = pos(c), q1 = pos(c == 0 ? H : N - c);
             float2 v[R2];
-            if (c == 0) {
 #pragma unroll
-                for (int k2 = 0; k2 < R2; ++k2) {
-                    const int j = k1 + R1 * k2;
-                    const float2 a = spec_at<SIGNED>(spec, j, 0, qf, cc);
-                    const float2 b = spec_at<SIGNED>(spec, j, H, qf, cc);
-                    v[k2] = make_float2(a.x - b.y, a.y + b.x);     // S0 + i S_{N/2}
-                }
-            } else {
-#pragma unroll
-                for (int k2 = 0; k2 < R2; ++k2)
-                    v[k2] = spec_at<SIGNED>(spec, k1 + R1 * k2, c, qf, cc);
-            }
+            for (int k2 = 0; k2 < R2; ++k2)
+                v[k2] = S[addr((R2 * k1 + k2) >> 1, (k2 & 1) ? q1 : q0)];
             cols_inverse1_store(S, W, c, k1, v);
         }
     }
@@ -465,13 +490,13 @@ __global__ void __launch_bounds__(2 * N, N == 128 ? 2 : 4) lowpass_fft_kernel(
     __shared__ float2 W[N];
     __shared__ double red[F::NT / 32];
     F::twiddles(W, twid);
-    if (!LOOP) {
+    if constexpr (!LOOP) {
         lowpass_image<N>(blockIdx.x, S, W, red, stack, num_stack, sidx, flip, gtab, xbuf, status);
-        return;
-    }
-    for (int64_t img = blockIdx.x; img < n_images; img += gridDim.x) {
-        __syncthreads();                               // S and red free from the last image
-        lowpass_image<N>(img, S, W, red, stack, num_stack, sidx, flip, gtab, xbuf, status);
+    } else {
+        for (int64_t img = blockIdx.x; img < n_images; img += gridDim.x) {
+            __syncthreads();                           // S and red free from the last image
+            lowpass_image<N>(img, S, W, red, stack, num_stack, sidx, flip, gtab, xbuf, status);
+        }
     }
 }
 

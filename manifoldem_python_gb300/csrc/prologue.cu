@@ -844,52 +844,58 @@ __global__ void __launch_bounds__(256) features_kernel(
     const int64_t K4 = 4 * Kc_pad;
     float2* sp = spec + img * Kc;
     KSum acc;
-#pragma unroll 2
-    for (int64_t k = threadIdx.x; k < Kc_pad; k += 256) {
-        float fu = 0.f, fv = 0.f, fr = 0.f, fs = 0.f;
-        const int64_t col = colmap[k];
-        if (k < Kc) {
-            const int ka = (int)(k / Nh), kb = (int)(k - (int64_t)ka * Nh);
-            const int fa = min(ka, N - ka);
-            const int m = fa * fa + kb * kb;
-            const bool w1 = (kb == 0 || ((N & 1) == 0 && kb == N / 2));
-            const float sw = w1 ? 1.0f : 1.41421356237309505f;
-            const float s2w = w1 ? 1.41421356237309505f : 2.0f;
-            const float2 F = sp[k];
-            if (spectrum_out) spectrum_out[img * Kc + k] = F;
-            int sg;
-            const float C = ctf_eval(m, qf, cc, &sg);
-            const float u = sw * (F.x * F.x + F.y * F.y);
-            const float v = sw * (C * C);
-            const float r = s2w * C * F.x;
-            const float s = s2w * C * F.y;
-            const float mu_u = mu[k], mu_v = mu[Kc_pad + k];
-            const float mu_r = mu[2 * Kc_pad + k], mu_s = mu[3 * Kc_pad + k];
-            acc.add(mu_u * v + mu_v * u - mu_u * mu_v - mu_r * r + 0.5f * mu_r * mu_r -
-                    mu_s * s + 0.5f * mu_s * mu_s);
-            fu = (u - mu_u) * sc;
-            fv = (v - mu_v) * sc;
-            fr = (r - mu_r) * sc;
-            fs = (s - mu_s) * sc;
-            if (write_signed) {
-                const float sgf = (float)sg * inv_nn;
-                sp[k] = make_float2(sgf * F.x, sgf * F.y);
-            }
+    // features (u', v', r', s') of frequency slot k; zero for the padding k >= Kc
+    auto feature = [&](int64_t k, float (&f)[4]) {
+        f[0] = f[1] = f[2] = f[3] = 0.f;
+        if (k >= Kc) return;
+        const int ka = (int)(k / Nh), kb = (int)(k - (int64_t)ka * Nh);
+        const int fa = min(ka, N - ka);
+        const int m = fa * fa + kb * kb;
+        const bool w1 = (kb == 0 || ((N & 1) == 0 && kb == N / 2));
+        const float sw = w1 ? 1.0f : 1.41421356237309505f;
+        const float s2w = w1 ? 1.41421356237309505f : 2.0f;
+        const float2 F = sp[k];
+        if (spectrum_out) spectrum_out[img * Kc + k] = F;
+        int sg;
+        const float C = ctf_eval(m, qf, cc, &sg);
+        const float u = sw * (F.x * F.x + F.y * F.y);
+        const float v = sw * (C * C);
+        const float r = s2w * C * F.x;
+        const float s = s2w * C * F.y;
+        const float mu_u = mu[k], mu_v = mu[Kc_pad + k];
+        const float mu_r = mu[2 * Kc_pad + k], mu_s = mu[3 * Kc_pad + k];
+        acc.add(mu_u * v + mu_v * u - mu_u * mu_v - mu_r * r + 0.5f * mu_r * mu_r -
+                mu_s * s + 0.5f * mu_s * mu_s);
+        f[0] = (u - mu_u) * sc;
+        f[1] = (v - mu_v) * sc;
+        f[2] = (r - mu_r) * sc;
+        f[3] = (s - mu_s) * sc;
+        if (write_signed) {
+            const float sgf = (float)sg * inv_nn;
+            sp[k] = make_float2(sgf * F.x, sgf * F.y);
         }
-        const float vals[4] = {fu, fv, fr, fs};
+    };
+    // two consecutive slots per thread: they share a 64-wide chunk, so their feature columns
+    // are adjacent (col even) and each block gets one paired store
+    for (int64_t k = 2 * (int64_t)threadIdx.x; k < Kc_pad; k += 512) {
+        float f0[4], f1[4];
+        feature(k, f0);
+        feature(k + 1, f1);
+        const int64_t col = colmap[k];
         if (MODE == 1) {
-            __nv_bfloat16* hi = (__nv_bfloat16*)feat_a + row * K4;
-            __nv_bfloat16* lo = (__nv_bfloat16*)feat_b + row * K4;
+            __nv_bfloat162* hi = (__nv_bfloat162*)((__nv_bfloat16*)feat_a + row * K4);
+            __nv_bfloat162* lo = (__nv_bfloat162*)((__nv_bfloat16*)feat_b + row * K4);
 #pragma unroll
             for (int b = 0; b < 4; ++b) {
-                const __nv_bfloat16 h = __float2bfloat16_rn(vals[b]);
-                hi[b * Kc_pad + col] = h;
-                lo[b * Kc_pad + col] = __float2bfloat16_rn(vals[b] - __bfloat162float(h));
+                const __nv_bfloat162 h = __floats2bfloat162_rn(f0[b], f1[b]);
+                const float2 hf = __bfloat1622float2(h);
+                hi[(b * Kc_pad + col) >> 1] = h;
+                lo[(b * Kc_pad + col) >> 1] = __floats2bfloat162_rn(f0[b] - hf.x, f1[b] - hf.y);
             }
         } else {
-            float* x = (float*)feat_a + row * K4;
+            float2* x = (float2*)((float*)feat_a + row * K4);
 #pragma unroll
-            for (int b = 0; b < 4; ++b) x[b * Kc_pad + col] = vals[b];
+            for (int b = 0; b < 4; ++b) x[(b * Kc_pad + col) >> 1] = make_float2(f0[b], f1[b]);
         }
     }
     const double a = block_sum_double<256>((double)acc.value(), red);

@@ -56,17 +56,20 @@ def read_spider_images(imgFileName: str, stack_index: np.ndarray, N: int):
     return imgs, inv.astype(np.int64)
 
 
-def assemble(job: PdJob, geom, res: Dict[str, np.ndarray], N: int, options: dict, msk2=1):
-    """The reference's output dict (keys, dtypes and shapes as written at :409-412)."""
+def assemble(job: PdJob, geom, res: Dict[str, np.ndarray], N: int, options: dict, msk2=1,
+             image_dtype=np.float64):
+    """The reference's output dict (keys, dtypes and shapes as written at :409-412).
+    ``image_dtype=np.float32`` (opt-in) keeps the per-image arrays CTF, imgAll and imgAllFlip
+    in the float32 the GPU computes them in, halving the pickle; keys and shapes are unchanged."""
     nS = job.ind.shape[0]
     avg_only = bool(options.get('avgOnly', False))
     D = res['D'] if not avg_only else np.zeros((nS, nS))
-    CTF = res['ctf'].astype(np.float64)
+    CTF = res['ctf'].astype(image_dtype)
     if not avg_only:
         CTF = CTF.reshape(nS, N * N)
-    vals = [D, job.ind, job.q, job.df, CTF, res['img_all'].astype(np.float64), msk2, geom.PD,
+    vals = [D, job.ind, job.q, job.df, CTF, res['img_all'].astype(image_dtype), msk2, geom.PD,
             geom.PDs, geom.Psis, res['img_avg'], res['img_avg_flip'],
-            res['img_all_flip'].astype(np.float64), geom.imgLabels, geom.Dnom, geom.Nom,
+            res['img_all_flip'].astype(image_dtype), geom.imgLabels, geom.Dnom, geom.Nom,
             res['img_all_intensity'], version, options]
     return dict(zip(OUTPUT_KEYS, vals))
 

@@ -84,3 +84,32 @@ def test_balanced_groups_cover_pds_in_order():
         if n_pd >= 100:
             sizes = [int(counts[list(g)].sum()) for g in groups]
             assert max(sizes) - min(sizes) <= 2 * counts.max()
+
+
+def test_async_writer_writes_pickles_then_markers(tmp_path):
+    """myio.AsyncWriter: every queued pickle is complete and readable with the reference's
+    format, each marker exists only with its pickle, and a bound on queued bytes does not
+    deadlock a single oversized item."""
+    import numpy as np
+    from manifoldem_python_gb300 import myio
+    keys = ['D', 'imgAll', 'ind']
+    with myio.AsyncWriter(workers=3, max_pending_bytes=1 << 20) as w:
+        for i in range(12):
+            vals = [np.full((50, 50), float(i)), np.zeros((4, 300, 300), np.float32) + i,
+                    np.arange(i)]
+            w.submit(str(tmp_path / ('pd_%d.pkl' % i)), keys, vals,
+                     marker=str(tmp_path / ('%d' % i)))
+    for i in range(12):
+        d = myio.fin1(str(tmp_path / ('pd_%d.pkl' % i)))
+        assert set(d) == set(keys) and float(d['D'][3, 4]) == i
+        assert d['imgAll'].dtype == np.float32 and (tmp_path / ('%d' % i)).exists()
+
+
+def test_async_writer_reraises(tmp_path):
+    import numpy as np
+    import pytest
+    from manifoldem_python_gb300 import myio
+    w = myio.AsyncWriter(workers=2)
+    w.submit(str(tmp_path / 'missing_dir' / 'x.pkl'), ['a'], [np.zeros(3)])
+    with pytest.raises(FileNotFoundError):
+        w.close()
