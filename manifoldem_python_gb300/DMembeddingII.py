@@ -114,7 +114,8 @@ def op(D, k: int, tune: float, prefsigma: float, num_eigs: int = NUM_EIGS,
     s0 = torch.empty(1, dtype=torch.float64, device=g.dev)
     g.call('mem_dm_sweep', Y.data_ptr(), n, scale.data_ptr(), 1, math.inf, s0.data_ptr())
     thr = max(-math.log(0.01 * float(s0.item()) / n_edges), 10.0)
-    scale = torch.from_numpy((log2e / (2.0 * np.exp(log_eps))).astype(np.float32)).to(g.dev)
+    with np.errstate(over='ignore'):     # +inf for the smallest eps: only d = 0 terms survive
+        scale = torch.from_numpy((log2e / (2.0 * np.exp(log_eps))).astype(np.float32)).to(g.dev)
     sums = torch.empty(len(log_eps), dtype=torch.float64, device=g.dev)
     g.call('mem_dm_sweep', Y.data_ptr(), n, scale.data_ptr(), len(log_eps), thr, sums.data_ptr())
     log_sum = np.log(sums.cpu().numpy())

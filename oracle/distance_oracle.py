@@ -163,8 +163,18 @@ def read_image(stack, idx: int, N: int) -> np.ndarray:
     return np.array(tmp.T, dtype=np.float32)
 
 
-def load_pd_images(stack, ind: np.ndarray, nStot: int, N: int, msk: np.ndarray):
-    """Images of one PD with conjugates flipped and background-normalised (``:245-283``).
+def read_image_relion(stack, idx: int, sh) -> np.ndarray:
+    """RELION image ``idx`` as the stage sees it (``:259-264``): the MRC stack's image as stored
+    (no transpose), shifted by (sh[1][idx] - 0.5, sh[0][idx] - 0.5) with
+    ``scipy.ndimage.shift(order=3, mode='wrap')``.  ``stack``: array (num_part, N, N)."""
+    from scipy.ndimage import shift
+    tmp = np.asarray(stack)[idx]
+    return shift(tmp, (sh[1][idx] - 0.5, sh[0][idx] - 0.5), order=3, mode='wrap')
+
+
+def load_pd_images(stack, ind: np.ndarray, nStot: int, N: int, msk: np.ndarray, sh=None):
+    """Images of one PD with conjugates flipped and background-normalised (``:245-283``);
+    ``sh`` = (shx, shy) selects the RELION branch (``read_image_relion``).
 
     Returns (images (nS, N, N) float64, imgLabels (nS,) int)."""
     nS = ind.shape[0]
@@ -177,7 +187,7 @@ def load_pd_images(stack, ind: np.ndarray, nStot: int, N: int, msk: np.ndarray):
         else:
             idx = int(ind[iS] - nStot / 2)
             labels[iS] = -1
-        tmp = read_image(stack, idx, N)
+        tmp = read_image(stack, idx, N) if sh is None else read_image_relion(stack, idx, sh)
         if ind[iS] >= nStot / 2:
             tmp = np.flipud(tmp)
         backg = tmp * (1 - msk)
@@ -191,17 +201,19 @@ def load_pd_images(stack, ind: np.ndarray, nStot: int, N: int, msk: np.ndarray):
 def pd_op(ind: np.ndarray, q: np.ndarray, df: np.ndarray, stack, nStot: int, *, N: int,
           pix_size: float, Cs: float, EkV: float, AmpContrast: float, gaussEnv: float = np.inf,
           filterPar: Optional[dict] = None, options: Optional[dict] = None,
-          psi_p: Optional[float] = None, msk2=1) -> Dict[str, object]:
+          psi_p: Optional[float] = None, msk2=1, sh=None) -> Dict[str, object]:
     """The 19 outputs of one PD (``getDistanceCTF_local_Conj9combinedS2.op`` ``:216-412``).
 
-    ``psi_p`` may be passed in to skip the least-squares fit (it is then used as given)."""
+    ``psi_p`` may be passed in to skip the least-squares fit (it is then used as given);
+    ``sh`` = (shx, shy) per stack image selects the RELION branch (``stack`` is then the MRC
+    stack's (num_part, N, N) array)."""
     filterPar = filterPar or dict(type='Butter', Qc=0.5, N=8)
     options = options if options is not None else dict(verbose=False, avgOnly=False, visual=False,
                                                         parallel=False, relion_data=False,
                                                         thres=None)
     nS = ind.shape[0]
     msk = annular_mask(0, N / 2., N, N)
-    imgs, imgLabels = load_pd_images(stack, ind, nStot, N, msk)
+    imgs, imgLabels = load_pd_images(stack, ind, nStot, N, msk, sh)
 
     # Butterworth low-pass of every image (:286-293)
     Q = create_grid(N)

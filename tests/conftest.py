@@ -9,7 +9,8 @@ GOLDEN = os.path.join(REPO, 'tests', 'golden')
 if REPO not in sys.path:
     sys.path.insert(0, REPO)
 
-GOLDEN_CASES = ['even32_conj', 'odd33_env', 'even32_avgonly', 'even48_neardup', 'config1']
+GOLDEN_CASES = ['even32_conj', 'odd33_env', 'even32_avgonly', 'even48_neardup', 'config1',
+                'relion32']
 
 
 def pytest_configure(config):
@@ -23,7 +24,16 @@ def load_golden(case):
 
 def golden_options(g):
     return dict(verbose=False, avgOnly=bool(g['avgOnly']), visual=False, parallel=False,
-                relion_data=False, thres=6000)
+                relion_data=golden_relion(g), thres=6000)
+
+
+def golden_relion(g):
+    return bool(g['relion']) if 'relion' in g else False
+
+
+def golden_shifts(g):
+    """(shx, shy) of a RELION case, else None."""
+    return (g['shx'], g['shy']) if golden_relion(g) else None
 
 
 def golden_micro(g):

@@ -35,7 +35,20 @@ def load_reference():
     mpl.pyplot = types.ModuleType('matplotlib.pyplot')
     sys.modules.setdefault('matplotlib', mpl)
     sys.modules.setdefault('matplotlib.pyplot', mpl.pyplot)
-    sys.modules.setdefault('mrcfile', types.ModuleType('mrcfile'))
+    # mrcfile stand-in: mmap(name).data is the stack as stored (the only use, :259-262)
+    sys.path.insert(0, REPO)
+    from manifoldem_python_gb300 import mrc
+    mrcfile = types.ModuleType('mrcfile')
+
+    class _Mmap:
+        def __init__(self, name, mode='r'):
+            self.data = mrc.read_stack(name)
+
+        def is_image_stack(self):
+            return True
+
+    mrcfile.mmap = _Mmap
+    sys.modules.setdefault('mrcfile', mrcfile)
     for d in (REF_MODULES, os.path.join(REF_MODULES, 'CC')):
         if d not in sys.path:
             sys.path.insert(0, d)
@@ -67,6 +80,10 @@ CASES = {
                        [0, 7, 39]),
     # the CPU-runnable workload: one PD, 300 images of 70x70 px
     'config1': (dict(N=70, n_pd=1, n_fixed=300, seed=11), {}, {}, [0, 1, 150, 299]),
+    # RELION branch: MRC stack read as stored, per-particle shifts (order-3 'wrap' shift),
+    # half of the PD conjugate views
+    'relion32': (dict(N=32, n_pd=1, n_fixed=14, conj_pd_frac=1.0, seed=105), {},
+                 dict(relion_data=True), None),
 }
 
 FULL_KEEP = ['D', 'ind', 'q', 'df', 'CTF', 'imgAll', 'PD', 'PDs', 'Psis', 'imgAvg',
@@ -92,9 +109,18 @@ def make_case(name):
                    relion_data=False, thres=6000)
     options.update(opt_over)
     filterPar = dict(type='Butter', Qc=0.5, N=8)
+    sh = ds.sh
+    if options['relion_data']:
+        rng = np.random.default_rng(cfg.seed + 7)
+        sh = (rng.uniform(-2.5, 2.5, stack.shape[0]), rng.uniform(-2.5, 2.5, stack.shape[0]))
     with tempfile.TemporaryDirectory() as tmp:
         stack_file = os.path.join(tmp, 'stack.bin')
-        stack.tofile(stack_file)
+        if options['relion_data']:
+            from manifoldem_python_gb300 import mrc
+            stack_file = os.path.join(tmp, 'stack.mrcs')
+            mrc.write_stack(stack_file, stack)
+        else:
+            stack.tofile(stack_file)
         ref_p.init()
         ref_p.nPix = cfg.N
         ref_p.pix_size = mic['pix_size']
@@ -106,14 +132,15 @@ def make_case(name):
         ref_p.dist_prog = os.path.join(tmp, 'progress')
         os.makedirs(ref_p.dist_prog)
         out_file = os.path.join(tmp, 'IMGs_prD_0')
-        ref_op.op([ind, q, df, out_file, 0], filterPar, stack_file, ds.sh, ds.nStot, options)
+        ref_op.op([ind, q, df, out_file, 0], filterPar, stack_file, sh, ds.nStot, options)
         with open(out_file, 'rb') as f:
             res = pickle.load(f)
         assert os.path.exists(os.path.join(ref_p.dist_prog, '0'))
     rec = dict(stack16=stack16, ind=ind, q=q, df=df, nStot=np.int64(ds.nStot), N=np.int64(cfg.N),
                pix_size=mic['pix_size'], Cs=mic['Cs'], EkV=mic['EkV'],
                AmpContrast=mic['AmpContrast'], gaussEnv=mic['gaussEnv'],
-               avgOnly=np.bool_(options['avgOnly']),
+               avgOnly=np.bool_(options['avgOnly']), relion=np.bool_(options['relion_data']),
+               shx=np.asarray(sh[0], dtype=np.float64), shy=np.asarray(sh[1], dtype=np.float64),
                ref_version=np.array(res['version']), ref_msk2=np.array(res['msk2']),
                ref_CTF_shape=np.array(np.shape(res['CTF'])))
     for k in FULL_KEEP:

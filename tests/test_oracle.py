@@ -3,7 +3,8 @@ import numpy as np
 import pytest
 from scipy import ndimage
 
-from conftest import GOLDEN_CASES, golden_micro, golden_options, golden_ref, load_golden
+from conftest import (GOLDEN_CASES, golden_micro, golden_options, golden_ref, golden_shifts,
+                      load_golden)
 from oracle import distance_oracle as O
 
 KEYS = ['D', 'CTF', 'imgAll', 'imgAllFlip', 'PD', 'PDs', 'Psis', 'imgAvg', 'imgAvgFlip',
@@ -14,7 +15,7 @@ KEYS = ['D', 'CTF', 'imgAll', 'imgAllFlip', 'PD', 'PDs', 'Psis', 'imgAvg', 'imgA
 def oracle_run(request):
     g = load_golden(request.param)
     res = O.pd_op(g['ind'], g['q'], g['df'], g['stack16'].astype(np.float32), int(g['nStot']),
-                  options=golden_options(g), **golden_micro(g))
+                  options=golden_options(g), sh=golden_shifts(g), **golden_micro(g))
     return request.param, g, res
 
 
