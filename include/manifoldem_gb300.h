@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define MEM_ABI_VERSION 1
+#define MEM_ABI_VERSION 2
 
 /* status codes */
 #define MEM_OK                    0
@@ -85,6 +85,11 @@ typedef struct mem_inputs {
     const uint8_t* flip;         /* [n_images] 1 for conjugate views (ind >= nStot/2)         */
     const double*  psi_rad;      /* [n_images] Psi_i = 2 atan(s/c), NaN replaced by 0 (:317-321) */
     const double*  df;           /* [n_images] defocus, Angstrom                               */
+    const double*  shift_yx;     /* NULL: SPIDER stack (image idx is the stored N x N block,
+                                    transposed, :254-257).  Else RELION stack (:259-264): the
+                                    stored image as is, shifted by [n_images][2] =
+                                    (sh_y - 0.5, sh_x - 0.5) of its particle with the order-3
+                                    'wrap' spline shift of scipy.ndimage; N <= 236            */
 } mem_inputs;
 
 /* Per-call device outputs; any pointer may be NULL to skip that output.                   */

@@ -18,7 +18,7 @@ from typing import List, Optional
 import numpy as np
 
 from . import myio, set_params
-from .getDistanceCTF_local_Conj9combinedS2 import (OUTPUT_KEYS, assemble, read_spider_images,
+from .getDistanceCTF_local_Conj9combinedS2 import (OUTPUT_KEYS, assemble, load_images,
                                                     stage_params)
 from .p import params_module
 from .pipeline import DEFAULT_OUTPUTS, DistanceStage, PdJob, admit_batches
@@ -56,7 +56,7 @@ def count(N) -> int:
 def run_jobs(jobs: list, stack_file: str, nStot: int, options: dict, progress=None,
              budget_bytes: Optional[int] = None, precision: Optional[str] = None,
              done_offset: int = 0, total: Optional[int] = None, writers: int = 4,
-             image_dtype=np.float64) -> None:
+             image_dtype=np.float64, sh=None) -> None:
     """Run ``jobs`` ([ind, q, df, outFile, prD] each) in HBM-admitted GPU batches; the pickles
     and markers of a batch are written by ``writers`` threads while the next batch computes
     (``writers=0``: written in line, as the reference does).  Progress is reported per PD when
@@ -77,14 +77,14 @@ def run_jobs(jobs: list, stack_file: str, nStot: int, options: dict, progress=No
     try:
         for batch in admit_batches(counts, params, budget_bytes):
             done = _run_batch(stage, params, jobs, batch, stack_file, nStot, options, N, p,
-                              writer, image_dtype, progress, done, total)
+                              writer, image_dtype, progress, done, total, sh)
     finally:
         if writer is not None:
             writer.close()
 
 
 def _run_batch(stage, params, jobs, batch, stack_file, nStot, options, N, p, writer,
-               image_dtype, progress, done, total):
+               image_dtype, progress, done, total, sh=None):
     """One HBM-admitted batch: read its images, run the stage, queue its pickles."""
     import torch
     pj = [PdJob(ind=np.asarray(jobs[i][0]), q=np.asarray(jobs[i][1], dtype=np.float64),
@@ -92,13 +92,13 @@ def _run_batch(stage, params, jobs, batch, stack_file, nStot, options, N, p, wri
                 prD=jobs[i][4]) for i in batch]
     geoms = stage.geometry(pj, nStot)
     all_idx = np.concatenate([g.stack_index for g in geoms])
-    imgs, compact = read_spider_images(stack_file, all_idx, N)
+    imgs, compact, sh_c = load_images(stack_file, all_idx, N, options, sh)
     off = 0
     for g in geoms:
         g.stack_index = compact[off:off + g.stack_index.size]
         off += g.stack_index.size
     stack = torch.from_numpy(imgs).to(stage.device)
-    results = stage.run(pj, stack, nStot, outputs=DEFAULT_OUTPUTS, geoms=geoms)
+    results = stage.run(pj, stack, nStot, outputs=DEFAULT_OUTPUTS, geoms=geoms, sh=sh_c)
     for job, geom, res in zip(pj, geoms, results):
         out = assemble(job, geom, res, N, options, image_dtype=image_dtype)
         marker = os.path.join(p.dist_prog, '%s' % job.prD)
@@ -122,6 +122,7 @@ def op(*argv):
     CG = data['CG']
     df = data['df']
     q = data['q']
+    sh = data.get('sh')
     size = len(df)
     options = dict(verbose=False, avgOnly=False, visual=False, parallel=False,
                    relion_data=p.relion_data, thres=p.PDsizeThH)
@@ -142,6 +143,6 @@ def op(*argv):
     print("Processing {} projection directions.".format(len(input_data)))
     if input_data:
         run_jobs(input_data, p.img_stack_file, size, options, progress=progress,
-                 done_offset=offset, total=p.numberofJobs)
+                 done_offset=offset, total=p.numberofJobs, sh=sh)
     set_params.op(0)
     return

@@ -22,7 +22,7 @@ INCLUDE = os.path.join(REPO, 'include')
 BUILD_DIR = os.path.join(REPO, '_build')
 LIB_PATH = os.path.join(HERE, 'libmanifoldem_gb300.so')
 SOURCES = ['abi.cu', 'prologue.cu', 'gemm_fp32.cu', 'gemm_tc.cu', 'noalloc.cu', 'image_fft.cu',
-           'dmap.cu']
+           'dmap.cu', 'relion.cu']
 ARCH_FLAGS = ['-gencode', 'arch=compute_103a,code=sm_103a']
 
 # status codes (include/manifoldem_gb300.h)
@@ -112,9 +112,13 @@ class MemParams(ctypes.Structure):
                 ('avg_only', c_int32), ('precision', c_int32)]
 
 
+ABI_VERSION = 2            # MEM_ABI_VERSION of include/manifoldem_gb300.h these structs follow
+
+
 class MemInputs(ctypes.Structure):
     _fields_ = [('stack', c_void_p), ('num_stack', c_int64), ('stack_index', c_void_p),
-                ('flip', c_void_p), ('psi_rad', c_void_p), ('df', c_void_p)]
+                ('flip', c_void_p), ('psi_rad', c_void_p), ('df', c_void_p),
+                ('shift_yx', c_void_p)]
 
 
 class MemOutputs(ctypes.Structure):
@@ -175,6 +179,9 @@ def load(path: Optional[str] = None) -> ctypes.CDLL:
             fn = getattr(lib, name)
             fn.restype = res
             fn.argtypes = args
+        if lib.mem_abi_version() != ABI_VERSION:
+            raise LibraryNotBuilt('%s has ABI version %d, expected %d: rebuild it'
+                                  % (path, lib.mem_abi_version(), ABI_VERSION))
         _lib = lib
         return lib
 

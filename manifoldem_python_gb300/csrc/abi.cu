@@ -306,6 +306,7 @@ int mem_plan_create(const mem_params* params, int32_t n_pd, const int32_t* pd_co
     L.pd_max = take(sizeof(uint32_t) * n_pd);
     L.colmap = take(sizeof(int32_t) * P->Kc_pad);
     L.twid = take(sizeof(float) * 2 * (P->N / 2 + 1));
+    L.ident = take(sizeof(int64_t) * P->n_images);      // 0..n-1: stack index of shifted copies
     L.xbuf = take(sizeof(float) * NN * P->n_images);
     L.spec = take(sizeof(float) * 2 * P->Kc * P->n_images);
     L.feat_a = take(feat_elem * 4 * P->Kc_pad * P->n_rows);
@@ -363,6 +364,12 @@ int mem_plan_upload(mem_plan* plan, void* workspace, size_t workspace_bytes, voi
                                  sizeof(Tile) * P.tiles.size(), cudaMemcpyHostToDevice, s));
     MEM_CUDA_TRY(cudaMemcpyAsync(at<char>(workspace, L.colmap), P.colmap.data(),
                                  sizeof(int32_t) * P.Kc_pad, cudaMemcpyHostToDevice, s));
+    {
+        std::vector<int64_t> ident(P.n_images);
+        for (int64_t i = 0; i < P.n_images; ++i) ident[i] = i;
+        MEM_CUDA_TRY(cudaMemcpyAsync(at<char>(workspace, L.ident), ident.data(),
+                                     sizeof(int64_t) * ident.size(), cudaMemcpyHostToDevice, s));
+    }
     // FFT twiddles exp(-2 pi i k / N), k = 0..N/2, computed in double
     std::vector<float> tw(2 * (P.N / 2 + 1));
     for (int k = 0; k <= P.N / 2; ++k) {
@@ -465,14 +472,24 @@ int execute_impl(mem_plan* plan, const mem_inputs* in, const mem_outputs* out, v
     MEM_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(uint32_t) * 4, ls));
     MEM_STEP(mark(0));
     MEM_STEP(kern::lowpass_table(P, at<float>(ws, L.gtab), ls));
+    mem_inputs lin = *in;
+    if (in->shift_yx) {
+        // RELION: shifted copies, laid out as SPIDER images, in the (still free) spectrum
+        // slots; the gather then reads copy i for entry i
+        float* shifted = reinterpret_cast<float*>(spec);
+        MEM_STEP(kern::relion_shift(P, *in, shifted, status, ls));
+        lin.stack = shifted;
+        lin.num_stack = P.n_images;
+        lin.stack_index = at<int64_t>(ws, L.ident);
+    }
     if (P.smem_fft) {
         // (a2, a3) gather, flip, normalisation and low-pass in one shared-memory pass
         MEM_STEP(mark(1));
-        MEM_STEP(kern::lowpass_fused(P, *in, at<float>(ws, L.gtab), at<float2>(ws, L.twid), xbuf,
-                                     status, load_ctas, ls));
+        MEM_STEP(kern::lowpass_fused(P, lin, at<float>(ws, L.gtab), at<float2>(ws, L.twid), xbuf,
+                                     status, in->shift_yx ? 0 : load_ctas, ls));
     } else {
         // (a2) gather, conjugate flip, normalisation
-        MEM_STEP(kern::gather_normalize(P, *in, xbuf, status, load_ctas, ls));
+        MEM_STEP(kern::gather_normalize(P, lin, xbuf, status, in->shift_yx ? 0 : load_ctas, ls));
         MEM_STEP(mark(1));
     }
     if (split) {

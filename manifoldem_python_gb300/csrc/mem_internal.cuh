@@ -62,7 +62,7 @@ __device__ __forceinline__ int ctf_sign(int m, uint64_t qf, const CtfConst& cc) 
 
 struct Layout {
     size_t status, pd_table, sum_items, img_pd, img_row, tiles;
-    size_t item_off, qfix, gtab, pd_max, colmap, twid;
+    size_t item_off, qfix, gtab, pd_max, colmap, twid, ident;
     size_t xbuf, spec, feat_a, feat_b, pair_norm, partial, means, avg_spec, avg_real, cufft_work;
     size_t total;
 };
@@ -120,6 +120,9 @@ int lowpass_table(const mem_plan& P, float* gtab, cudaStream_t s);
 int lowpass_fused(const mem_plan& P, const mem_inputs& in, const float* gtab,
                   const float2* twid, float* xbuf, uint32_t* status, int64_t max_ctas,
                   cudaStream_t s);
+// RELION read: shifted images, laid out as SPIDER stack images, into out [n_images][N][N]
+int relion_shift(const mem_plan& P, const mem_inputs& in, float* out, uint32_t* status,
+                 cudaStream_t s);
 // shared-memory real 2D FFTs (N = 32, 64, 128) with the layout and scaling of a cuFFT R2C/C2R
 int spectrum_fft(const mem_plan& P, int64_t count, const float* images, const float2* twid,
                  float2* spec, cudaStream_t s);

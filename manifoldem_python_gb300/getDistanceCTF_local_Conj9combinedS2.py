@@ -56,6 +56,25 @@ def read_spider_images(imgFileName: str, stack_index: np.ndarray, N: int):
     return imgs, inv.astype(np.int64)
 
 
+def read_relion_images(imgFileName: str, stack_index: np.ndarray, sh):
+    """Images ``stack_index`` of a RELION MRC stack as stored (``:259-262``), the compact index
+    of every entry, and the particles' shifts (shx, shy) in compact order."""
+    from . import mrc
+    data = mrc.read_stack(imgFileName)
+    uniq, inv = np.unique(stack_index, return_inverse=True)
+    imgs = np.ascontiguousarray(data[uniq], dtype=np.float32)
+    sh_c = (np.asarray(sh[0], dtype=np.float64)[uniq], np.asarray(sh[1], dtype=np.float64)[uniq])
+    return imgs, inv.astype(np.int64), sh_c
+
+
+def load_images(imgFileName: str, stack_index: np.ndarray, N: int, options: dict, sh):
+    """The stage's image input for either branch: (images, compact index, shifts or None)."""
+    if options.get('relion_data'):
+        return read_relion_images(imgFileName, stack_index, sh)
+    imgs, compact = read_spider_images(imgFileName, stack_index, N)
+    return imgs, compact, None
+
+
 def assemble(job: PdJob, geom, res: Dict[str, np.ndarray], N: int, options: dict, msk2=1,
              image_dtype=np.float64):
     """The reference's output dict (keys, dtypes and shapes as written at :409-412).
@@ -83,18 +102,16 @@ def op(input_data, filterPar, imgFileName, sh, nStot, options):
     q = np.asarray(q, dtype=np.float64)
     df = np.asarray(df, dtype=np.float64)
     N = int(p.nPix)
-    if options.get('relion_data'):
-        raise NotImplementedError('RELION (.mrcs) input is not supported by the GPU stage yet')
     if getattr(p, 'mask_vol_file', ''):
         raise NotImplementedError('volume masks (p.mask_vol_file) are not supported by the GPU '
                                   'stage yet')
     stage = DistanceStage(stage_params(p, filterPar, options))
     job = PdJob(ind=ind, q=q, df=df, outFile=outFile, prD=prD)
     geom = stage.geometry([job], nStot)[0]
-    imgs, compact = read_spider_images(imgFileName, geom.stack_index, N)
+    imgs, compact, sh_c = load_images(imgFileName, geom.stack_index, N, options, sh)
     geom.stack_index = compact
     stack = torch.from_numpy(imgs).to(stage.device)
-    res = stage.run([job], stack, nStot, outputs=DEFAULT_OUTPUTS, geoms=[geom])[0]
+    res = stage.run([job], stack, nStot, outputs=DEFAULT_OUTPUTS, geoms=[geom], sh=sh_c)[0]
     out = assemble(job, geom, res, N, options)
     myio.fout1(outFile, OUTPUT_KEYS, [out[k] for k in OUTPUT_KEYS])
     progress_fname = os.path.join(p.dist_prog, '%s' % prD)

@@ -112,14 +112,16 @@ class Plan:
         return out
 
     def execute(self, stack, stack_index, flip, psi_rad, df, outputs: Dict[str, object],
-                stream=None) -> None:
+                stream=None, shift_yx=None) -> None:
         """Enqueue the stage on ``stream`` (default: torch's current stream).  All tensors
-        must be on the plan's device."""
+        must be on the plan's device.  ``shift_yx`` ([n_images, 2] float64): a RELION stack,
+        see ``relion_shifts``."""
         import torch
         stream = stream or torch.cuda.current_stream(self.device)
         cin = _lib.MemInputs(stack=stack.data_ptr(), num_stack=int(stack.shape[0]),
                              stack_index=stack_index.data_ptr(), flip=flip.data_ptr(),
-                             psi_rad=psi_rad.data_ptr(), df=df.data_ptr())
+                             psi_rad=psi_rad.data_ptr(), df=df.data_ptr(),
+                             shift_yx=_ptr(shift_yx))
         cout = _lib.MemOutputs(**{k: _ptr(outputs.get(k)) for k in OUTPUT_NAMES})
         self._keep = (cin, cout)
         _lib.check(self.lib.mem_plan_execute(self.handle, ctypes.byref(cin), ctypes.byref(cout),
@@ -133,7 +135,7 @@ class Plan:
         ``stream`` (mem_plan_execute_split); ``stack`` may be a pinned host tensor."""
         cin = _lib.MemInputs(stack=stack.data_ptr(), num_stack=int(stack.shape[0]),
                              stack_index=stack_index.data_ptr(), flip=flip.data_ptr(),
-                             psi_rad=psi_rad.data_ptr(), df=df.data_ptr())
+                             psi_rad=psi_rad.data_ptr(), df=df.data_ptr(), shift_yx=None)
         cout = _lib.MemOutputs(**{k: _ptr(outputs.get(k)) for k in OUTPUT_NAMES})
         self._keep = (cin, cout)
         _lib.check(self.lib.mem_plan_execute_split(
@@ -224,9 +226,10 @@ class DistanceStage:
                 for j in jobs]
 
     def run(self, jobs: Sequence[PdJob], stack, nStot: int, outputs=DEFAULT_OUTPUTS,
-            geoms: Optional[Sequence[PdGeometry]] = None, to_host: bool = True):
+            geoms: Optional[Sequence[PdGeometry]] = None, to_host: bool = True, sh=None):
         """Run every job; returns one dict per PD with host numpy (``to_host``) or device
-        arrays.  ``stack`` is a device tensor (num_part, N, N) float32 in SPIDER storage order."""
+        arrays.  ``stack`` is a device tensor (num_part, N, N) float32 in SPIDER storage order,
+        or, with ``sh`` = (shx, shy) per particle, the images of a RELION stack as stored."""
         import torch
         geoms = list(geoms) if geoms is not None else self.geometry(jobs, nStot)
         counts = [int(np.asarray(j.ind).shape[0]) for j in jobs]
@@ -238,10 +241,25 @@ class DistanceStage:
         df = torch.from_numpy(np.concatenate([np.asarray(j.df, dtype=np.float64).reshape(-1)
                                               for j in jobs])).to(dev)
         outs = plan.allocate_outputs(outputs)
-        plan.execute(stack, sidx, flip, psi, df, outs)
+        shifts = None
+        if sh is not None:
+            shifts = torch.from_numpy(relion_shifts(
+                np.concatenate([g.stack_index for g in geoms]), sh)).to(dev)
+        plan.execute(stack, sidx, flip, psi, df, outs, shift_yx=shifts)
         torch.cuda.synchronize(dev)
         plan.device_status()
         return split_outputs(plan, counts, outs, to_host)
+
+
+def relion_shifts(stack_index: np.ndarray, sh) -> np.ndarray:
+    """Per-entry shifts (axis 0, axis 1) = (sh_y - 0.5, sh_x - 0.5) of the entry's particle, the
+    arguments of the reference's scipy shift (``getDistanceCTF_local_Conj9combinedS2.py:263``);
+    ``sh`` = (shx, shy) indexed by particle."""
+    idx = np.asarray(stack_index, dtype=np.int64)
+    out = np.empty((idx.size, 2), dtype=np.float64)
+    out[:, 0] = np.asarray(sh[1], dtype=np.float64)[idx] - 0.5
+    out[:, 1] = np.asarray(sh[0], dtype=np.float64)[idx] - 0.5
+    return out
 
 
 def balanced_groups(counts: Sequence[int], n_groups: int) -> List[range]:

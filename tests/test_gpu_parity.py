@@ -14,7 +14,8 @@ import tempfile
 import numpy as np
 import pytest
 
-from conftest import GOLDEN_CASES, golden_micro, golden_options, golden_ref, load_golden
+from conftest import (GOLDEN_CASES, golden_micro, golden_options, golden_ref, golden_shifts,
+                      load_golden)
 
 pytestmark = pytest.mark.gpu
 
@@ -35,7 +36,7 @@ def run_case(torch, g, precision, outputs=None):
     stack = torch.from_numpy(g['stack16'].astype(np.float32)).cuda()
     outs = outputs or ('D', 'img_avg', 'img_avg_flip', 'img_all_intensity', 'img_all',
                        'img_all_flip', 'ctf', 'spectrum')
-    return stage.run([job], stack, int(g['nStot']), outputs=outs)[0]
+    return stage.run([job], stack, int(g['nStot']), outputs=outs, sh=golden_shifts(g))[0]
 
 
 @pytest.mark.parametrize('precision', PRECISIONS)

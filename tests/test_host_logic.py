@@ -113,3 +113,23 @@ def test_async_writer_reraises(tmp_path):
     w.submit(str(tmp_path / 'missing_dir' / 'x.pkl'), ['a'], [np.zeros(3)])
     with pytest.raises(FileNotFoundError):
         w.close()
+
+
+def test_mrc_round_trip(tmp_path):
+    """The MRC stack reader/writer used for RELION stacks: header fields, orientation (data is
+    (nz, ny, nx) as stored), and an extended header skipped by its declared length."""
+    import numpy as np
+    from manifoldem_python_gb300 import mrc
+    data = np.random.default_rng(0).standard_normal((3, 5, 4)).astype(np.float32)
+    path = str(tmp_path / 'a.mrcs')
+    mrc.write_stack(path, data)
+    h = mrc.read_header(path)
+    assert (h['nx'], h['ny'], h['nz'], h['mode']) == (4, 5, 3, 2)
+    np.testing.assert_array_equal(np.asarray(mrc.read_stack(path)), data)
+    raw = bytearray(open(path, 'rb').read())
+    ext = 2048
+    raw[92:96] = np.int32(ext).tobytes()
+    raw = raw[:1024] + bytes(ext) + raw[1024:]
+    path2 = str(tmp_path / 'b.mrcs')
+    open(path2, 'wb').write(bytes(raw))
+    np.testing.assert_array_equal(np.asarray(mrc.read_stack(path2)), data)
