@@ -60,6 +60,12 @@ def _hamilton(q: np.ndarray, s: np.ndarray) -> np.ndarray:
 
 def spider_psi(qr: np.ndarray) -> float:
     """Spider psi (radians) of a unit quaternion by the reference's least-squares fit."""
+    return spider_euler(qr)[2]
+
+
+def spider_euler(qr: np.ndarray):
+    """Spider (phi, theta, psi) in radians of a unit quaternion: the least-squares fit of
+    q2Spider.op (modules/q2Spider.py:19-60), same start, bounds and tolerance."""
     qr = qr / np.sqrt(sum(qr ** 2))
 
     def residual(a):
@@ -73,7 +79,33 @@ def spider_psi(qr: np.ndarray) -> float:
 
     res = optimize.least_squares(residual, np.array([0, 0, 0]), bounds=(-np.inf, np.inf),
                                  ftol=1e-12)
-    return res.x[2]
+    return res.x[0], res.x[1], res.x[2]
+
+
+def spider_rotation(phi: float, theta: float, psi: float) -> np.ndarray:
+    """Rotation matrix of Spider Euler angles (radians), projectMask.eulerRotMatrix3DSpider
+    (modules/projectMask.py:48-58)."""
+    cf, sf = np.cos(phi), np.sin(phi)
+    ct, st = np.cos(theta), np.sin(theta)
+    cp, sp = np.cos(psi), np.sin(psi)
+    return np.array([[cf * cp * ct - sf * sp, cp * ct * sf + cf * sp, -cp * st],
+                     [-cp * sf - cf * ct * sp, cf * cp - ct * sf * sp, sp * st],
+                     [cf * st, sf * st, ct]])
+
+
+def mask_transform(PD: np.ndarray, N: int):
+    """The affine map of projectMask.op (modules/projectMask.py:120-131) for projection
+    direction PD: output voxel o of the (axis-0/2 swapped) mask volume samples the input at
+    R o + offset.  Returns (R (3, 3), offset (3,))."""
+    Qr = np.array([1 + PD[2], PD[1], -PD[0], 0]).T
+    q1 = Qr / np.sqrt(sum(Qr ** 2))
+    phi, theta, psi = spider_euler(q1)
+    sym = np.array([phi, theta, psi])
+    sym[2] = 0
+    sym = sym * (-1.)
+    R = spider_rotation(sym[2], sym[1], sym[0])
+    c = 0.5 * np.array([N, N, N], dtype=np.float64)
+    return R, c - np.dot(R, c)
 
 
 def psi_ang(PD: np.ndarray) -> float:

@@ -197,16 +197,60 @@ def load_pd_images(stack, ind: np.ndarray, nStot: int, N: int, msk: np.ndarray, 
     return out, labels
 
 
+def project_mask(vol: np.ndarray, PD: np.ndarray) -> np.ndarray:
+    """projectMask.op (modules/projectMask.py:118-135): the mask volume rotated to the
+    projection direction (scipy affine_transform, order 3, mode 'nearest'), summed along z,
+    thresholded at 1; (N, N) bool."""
+    from scipy.ndimage import affine_transform
+    from scipy import optimize
+    vol = np.swapaxes(vol, 0, 2)
+    N = vol.shape[0]
+    # getEuler_from_PD (:93-108) with q2Spider.op's least-squares fit (q2Spider.py:19-60)
+    Qr = np.array([1 + PD[2], PD[1], -PD[0], 0]).T
+    q1 = Qr / np.sqrt(sum(Qr ** 2))
+
+    def qmul(q, s):
+        return np.array([q[0] * s[0] - q[1] * s[1] - q[2] * s[2] - q[3] * s[3],
+                         q[0] * s[1] + q[1] * s[0] + q[2] * s[3] - q[3] * s[2],
+                         q[0] * s[2] - q[1] * s[3] + q[2] * s[0] + q[3] * s[1],
+                         q[0] * s[3] + q[1] * s[2] - q[2] * s[1] + q[3] * s[0]])
+
+    def dev(a):
+        qa = np.array([np.cos(a[0] / 2.), 0., 0., -np.sin(a[0] / 2.)])
+        qb = np.array([np.cos(a[1] / 2.), 0, -np.sin(a[1] / 2.), 0.])
+        qc = np.array([np.cos(a[2] / 2.), 0., 0., -np.sin(a[2] / 2)])
+        return q1 - qmul(qc, qmul(qb, qa))
+
+    a = optimize.least_squares(dev, np.array([0, 0, 0]), bounds=(-np.inf, np.inf),
+                               ftol=1e-12).x
+    Phi, Theta, Psi = -0.0, -a[1], -a[0]            # sym = -[phi, theta, 0], (sym[2], sym[1], sym[0])
+    R = np.array([[np.cos(Phi) * np.cos(Psi) * np.cos(Theta) - np.sin(Phi) * np.sin(Psi),
+                   np.cos(Psi) * np.cos(Theta) * np.sin(Phi) + np.cos(Phi) * np.sin(Psi),
+                   -np.cos(Psi) * np.sin(Theta)],
+                  [-np.cos(Psi) * np.sin(Phi) - np.cos(Phi) * np.cos(Theta) * np.sin(Psi),
+                   np.cos(Phi) * np.cos(Psi) - np.cos(Theta) * np.sin(Phi) * np.sin(Psi),
+                   np.sin(Psi) * np.sin(Theta)],
+                  [np.cos(Phi) * np.sin(Theta), np.sin(Phi) * np.sin(Theta), np.cos(Theta)]])
+    c = 0.5 * np.array(vol.shape, dtype=np.float64)
+    offset = c - np.dot(R, c)
+    rho = affine_transform(input=vol, matrix=R, offset=offset, output_shape=vol.shape,
+                           mode='nearest')
+    msk = np.sum(rho, axis=2).reshape(N, N).T
+    return msk > 1
+
+
 # ----------------------------------------------------------------------------- the stage
 def pd_op(ind: np.ndarray, q: np.ndarray, df: np.ndarray, stack, nStot: int, *, N: int,
           pix_size: float, Cs: float, EkV: float, AmpContrast: float, gaussEnv: float = np.inf,
           filterPar: Optional[dict] = None, options: Optional[dict] = None,
-          psi_p: Optional[float] = None, msk2=1, sh=None) -> Dict[str, object]:
+          psi_p: Optional[float] = None, msk2=1, sh=None,
+          mask_volume=None) -> Dict[str, object]:
     """The 19 outputs of one PD (``getDistanceCTF_local_Conj9combinedS2.op`` ``:216-412``).
 
     ``psi_p`` may be passed in to skip the least-squares fit (it is then used as given);
     ``sh`` = (shx, shy) per stack image selects the RELION branch (``stack`` is then the MRC
-    stack's (num_part, N, N) array)."""
+    stack's (num_part, N, N) array); ``mask_volume`` (the volume of p.mask_vol_file) gives the
+    projected mask msk2 of the PD."""
     filterPar = filterPar or dict(type='Butter', Qc=0.5, N=8)
     options = options if options is not None else dict(verbose=False, avgOnly=False, visual=False,
                                                         parallel=False, relion_data=False,
@@ -227,6 +271,8 @@ def pd_op(ind: np.ndarray, q: np.ndarray, df: np.ndarray, stack, nStot: int, *, 
     PD = PD / np.linalg.norm(PD)
     if psi_p is None:
         psi_p = psi_ang(PD)
+    if mask_volume is not None:                          # (:303-310)
+        msk2 = project_mask(mask_volume, PD)
 
     Psis = np.nan * np.ones((nS, 1))
     Nom = np.nan * np.ones((nS, 1))

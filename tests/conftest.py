@@ -10,7 +10,7 @@ if REPO not in sys.path:
     sys.path.insert(0, REPO)
 
 GOLDEN_CASES = ['even32_conj', 'odd33_env', 'even32_avgonly', 'even48_neardup', 'config1',
-                'relion32']
+                'relion32', 'volmask32']
 
 
 def pytest_configure(config):
@@ -29,6 +29,12 @@ def golden_options(g):
 
 def golden_relion(g):
     return bool(g['relion']) if 'relion' in g else False
+
+
+def golden_mask_volume(g):
+    """The mask volume of a case run with p.mask_vol_file, else None."""
+    v = g.get('mask_volume')
+    return v.astype(np.float32) if v is not None and v.size else None
 
 
 def golden_shifts(g):

@@ -47,8 +47,23 @@ def load_reference():
         def is_image_stack(self):
             return True
 
+    class _Open(_Mmap):
+        def __enter__(self):
+            return self
+
+        def __exit__(self, *exc):
+            return False
+
     mrcfile.mmap = _Mmap
+    mrcfile.open = _Open
     sys.modules.setdefault('mrcfile', mrcfile)
+    # projectMask imports these names from the third-party `transformations` module but its
+    # op() path (getEuler_from_PD, rotateVolumeEuler) does not call them
+    tr = types.ModuleType('transformations')
+    for name in ('euler_from_quaternion', 'quaternion_from_euler', 'quaternion_conjugate',
+                 'quaternion_matrix'):
+        setattr(tr, name, None)
+    sys.modules.setdefault('transformations', tr)
     for d in (REF_MODULES, os.path.join(REF_MODULES, 'CC')):
         if d not in sys.path:
             sys.path.insert(0, d)
@@ -84,7 +99,19 @@ CASES = {
     # half of the PD conjugate views
     'relion32': (dict(N=32, n_pd=1, n_fixed=14, conj_pd_frac=1.0, seed=105), {},
                  dict(relion_data=True), None),
+    # volume mask (p.mask_vol_file): projectMask's 2D mask multiplies the spectra and averages
+    'volmask32': (dict(N=32, n_pd=1, n_fixed=14, conj_pd_frac=1.0, seed=106),
+                  dict(volmask=True), {}, None),
 }
+
+
+def mask_volume(N):
+    """A binary mask volume: an off-centre ellipsoid (float32, (N, N, N))."""
+    z, y, x = np.meshgrid(*(np.arange(N, dtype=np.float64),) * 3, indexing='ij')
+    c = 0.5 * N
+    r = ((x - c - 2.) / (0.36 * N)) ** 2 + ((y - c + 1.) / (0.30 * N)) ** 2 + \
+        ((z - c) / (0.26 * N)) ** 2
+    return (r < 1).astype(np.float32)
 
 FULL_KEEP = ['D', 'ind', 'q', 'df', 'CTF', 'imgAll', 'PD', 'PDs', 'Psis', 'imgAvg',
              'imgAvgFlip', 'imgAllFlip', 'imgLabels', 'Dnom', 'Nom', 'imgAllIntensity']
@@ -104,6 +131,7 @@ def make_case(name):
     q = ds.q[:, ind]
     df = ds.df[ind]
     mic = dict(pix_size=cfg.pix, Cs=cfg.cs, EkV=cfg.kv, AmpContrast=cfg.ampc, gaussEnv=np.inf)
+    volmask = bool(mic_over.pop('volmask', False)) if mic_over else False
     mic.update(mic_over)
     options = dict(verbose=False, avgOnly=False, visual=False, parallel=False,
                    relion_data=False, thres=6000)
@@ -129,6 +157,12 @@ def make_case(name):
         ref_p.AmpContrast = mic['AmpContrast']
         ref_p.gaussEnv = mic['gaussEnv']
         ref_p.mask_vol_file = ''
+        mvol = None
+        if volmask:
+            from manifoldem_python_gb300 import mrc
+            mvol = mask_volume(cfg.N)
+            ref_p.mask_vol_file = os.path.join(tmp, 'mask.mrc')
+            mrc.write_stack(ref_p.mask_vol_file, mvol)
         ref_p.dist_prog = os.path.join(tmp, 'progress')
         os.makedirs(ref_p.dist_prog)
         out_file = os.path.join(tmp, 'IMGs_prD_0')
@@ -142,6 +176,7 @@ def make_case(name):
                avgOnly=np.bool_(options['avgOnly']), relion=np.bool_(options['relion_data']),
                shx=np.asarray(sh[0], dtype=np.float64), shy=np.asarray(sh[1], dtype=np.float64),
                ref_version=np.array(res['version']), ref_msk2=np.array(res['msk2']),
+               mask_volume=(mvol.astype(np.uint8) if mvol is not None else np.zeros(0, np.uint8)),
                ref_CTF_shape=np.array(np.shape(res['CTF'])))
     for k in FULL_KEEP:
         if slice_idx is not None and k in SLICE_KEYS:

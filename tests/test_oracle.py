@@ -3,8 +3,8 @@ import numpy as np
 import pytest
 from scipy import ndimage
 
-from conftest import (GOLDEN_CASES, golden_micro, golden_options, golden_ref, golden_shifts,
-                      load_golden)
+from conftest import (GOLDEN_CASES, golden_mask_volume, golden_micro, golden_options,
+                      golden_ref, golden_shifts, load_golden)
 from oracle import distance_oracle as O
 
 KEYS = ['D', 'CTF', 'imgAll', 'imgAllFlip', 'PD', 'PDs', 'Psis', 'imgAvg', 'imgAvgFlip',
@@ -15,7 +15,8 @@ KEYS = ['D', 'CTF', 'imgAll', 'imgAllFlip', 'PD', 'PDs', 'Psis', 'imgAvg', 'imgA
 def oracle_run(request):
     g = load_golden(request.param)
     res = O.pd_op(g['ind'], g['q'], g['df'], g['stack16'].astype(np.float32), int(g['nStot']),
-                  options=golden_options(g), sh=golden_shifts(g), **golden_micro(g))
+                  options=golden_options(g), sh=golden_shifts(g),
+                  mask_volume=golden_mask_volume(g), **golden_micro(g))
     return request.param, g, res
 
 
@@ -34,7 +35,7 @@ def test_oracle_matches_reference(oracle_run):
             assert np.abs(mine - ref).max() / den < 1e-12, (case, k)
     assert tuple(g['ref_CTF_shape']) == np.shape(res['CTF'])
     assert str(g['ref_version']) == res['version']
-    assert int(g['ref_msk2']) == res['msk2']
+    np.testing.assert_array_equal(np.asarray(res['msk2']), g['ref_msk2'])
 
 
 def test_rotation_is_periodic_bspline():
