@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define MEM_ABI_VERSION 2
+#define MEM_ABI_VERSION 3
 
 /* status codes */
 #define MEM_OK                    0
@@ -90,6 +90,9 @@ typedef struct mem_inputs {
                                     stored image as is, shifted by [n_images][2] =
                                     (sh_y - 0.5, sh_x - 0.5) of its particle with the order-3
                                     'wrap' spline shift of scipy.ndimage; N <= 236            */
+    const uint8_t* pd_mask;      /* NULL, or [n_pd][N][N] projected volume mask msk2 of every PD
+                                    (mem_mask_project; reference :303-310): multiplies each
+                                    rotated image before its spectrum (:344)                  */
 } mem_inputs;
 
 /* Per-call device outputs; any pointer may be NULL to skip that output.                   */
@@ -214,6 +217,20 @@ int mem_dm_symmetrise(const double* D, int64_t n, const uint8_t* listed, double*
 int mem_dm_sweep(const double* Y, int64_t n, const float* scale, int32_t n_eps, double thr,
                  double* sums, void* stream);
 int mem_dm_laplacian(double* Y, int64_t n, double sigma, double* scratch, void* stream);
+
+/* ---- volume mask (reference :303-310, projectMask.op modules/projectMask.py:118-135) ------
+ * mem_mask_prepare: spline coefficients of the mask volume (device, (N, N, N) float32 as
+ *   stored, z y x) for projectMask's order-3 'nearest' affine_transform: axes 0 and 2 swapped,
+ *   padded by 12 edge samples per side, 'reflect' prefiltered; coeffs holds
+ *   mem_mask_coefficients_size bytes (float64, (N+24)^3).  N <= 236.
+ * mem_mask_project: for every PD p, masks[p] (N x N bytes, 0/1) = projectMask.op of the volume:
+ *   transforms[p] = R row-major (9 doubles) and offset (3) of the PD's affine map (output voxel
+ *   o samples the volume at R o + offset; manifoldem_python_gb300.geometry.mask_transform);
+ *   device pointers.  Float64 throughout.                                                    */
+int mem_mask_coefficients_size(int32_t N, size_t* bytes);
+int mem_mask_prepare(const float* volume, int32_t N, double* coeffs, void* stream);
+int mem_mask_project(const double* coeffs, int32_t N, int32_t n_pd, const double* transforms,
+                     uint8_t* masks, void* stream);
 
 #ifdef __cplusplus
 }

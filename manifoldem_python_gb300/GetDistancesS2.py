@@ -19,7 +19,7 @@ import numpy as np
 
 from . import myio, set_params
 from .getDistanceCTF_local_Conj9combinedS2 import (OUTPUT_KEYS, assemble, load_images,
-                                                    stage_params)
+                                                    stage_params, volume_mask)
 from .p import params_module
 from .pipeline import DEFAULT_OUTPUTS, DistanceStage, PdJob, admit_batches
 from .sharding import shard
@@ -74,17 +74,18 @@ def run_jobs(jobs: list, stack_file: str, nStot: int, options: dict, progress=No
     done = done_offset
     total = total or len(jobs)
     writer = myio.AsyncWriter(writers) if writers > 0 else None
+    mask = volume_mask(p, stage.device)
     try:
         for batch in admit_batches(counts, params, budget_bytes):
             done = _run_batch(stage, params, jobs, batch, stack_file, nStot, options, N, p,
-                              writer, image_dtype, progress, done, total, sh)
+                              writer, image_dtype, progress, done, total, sh, mask)
     finally:
         if writer is not None:
             writer.close()
 
 
 def _run_batch(stage, params, jobs, batch, stack_file, nStot, options, N, p, writer,
-               image_dtype, progress, done, total, sh=None):
+               image_dtype, progress, done, total, sh=None, mask=None):
     """One HBM-admitted batch: read its images, run the stage, queue its pickles."""
     import torch
     pj = [PdJob(ind=np.asarray(jobs[i][0]), q=np.asarray(jobs[i][1], dtype=np.float64),
@@ -98,9 +99,11 @@ def _run_batch(stage, params, jobs, batch, stack_file, nStot, options, N, p, wri
         g.stack_index = compact[off:off + g.stack_index.size]
         off += g.stack_index.size
     stack = torch.from_numpy(imgs).to(stage.device)
-    results = stage.run(pj, stack, nStot, outputs=DEFAULT_OUTPUTS, geoms=geoms, sh=sh_c)
+    results = stage.run(pj, stack, nStot, outputs=DEFAULT_OUTPUTS, geoms=geoms, sh=sh_c,
+                        mask=mask)
     for job, geom, res in zip(pj, geoms, results):
-        out = assemble(job, geom, res, N, options, image_dtype=image_dtype)
+        out = assemble(job, geom, res, N, options, msk2=res.get('msk2', 1),
+                       image_dtype=image_dtype)
         marker = os.path.join(p.dist_prog, '%s' % job.prD)
         vals = [out[k] for k in OUTPUT_KEYS]
         if writer is not None:

@@ -22,7 +22,7 @@ INCLUDE = os.path.join(REPO, 'include')
 BUILD_DIR = os.path.join(REPO, '_build')
 LIB_PATH = os.path.join(HERE, 'libmanifoldem_gb300.so')
 SOURCES = ['abi.cu', 'prologue.cu', 'gemm_fp32.cu', 'gemm_tc.cu', 'noalloc.cu', 'image_fft.cu',
-           'dmap.cu', 'relion.cu']
+           'dmap.cu', 'relion.cu', 'mask.cu']
 ARCH_FLAGS = ['-gencode', 'arch=compute_103a,code=sm_103a']
 
 # status codes (include/manifoldem_gb300.h)
@@ -112,13 +112,13 @@ class MemParams(ctypes.Structure):
                 ('avg_only', c_int32), ('precision', c_int32)]
 
 
-ABI_VERSION = 2            # MEM_ABI_VERSION of include/manifoldem_gb300.h these structs follow
+ABI_VERSION = 3            # MEM_ABI_VERSION of include/manifoldem_gb300.h these structs follow
 
 
 class MemInputs(ctypes.Structure):
     _fields_ = [('stack', c_void_p), ('num_stack', c_int64), ('stack_index', c_void_p),
                 ('flip', c_void_p), ('psi_rad', c_void_p), ('df', c_void_p),
-                ('shift_yx', c_void_p)]
+                ('shift_yx', c_void_p), ('pd_mask', c_void_p)]
 
 
 class MemOutputs(ctypes.Structure):
@@ -150,6 +150,9 @@ SIGNATURES = {
     'mem_dm_sweep': (c_int32, [c_void_p, c_int64, c_void_p, c_int32, c_double, c_void_p,
                                c_void_p]),
     'mem_dm_laplacian': (c_int32, [c_void_p, c_int64, c_double, c_void_p, c_void_p]),
+    'mem_mask_coefficients_size': (c_int32, [c_int32, ctypes.POINTER(c_size_t)]),
+    'mem_mask_prepare': (c_int32, [c_void_p, c_int32, c_void_p, c_void_p]),
+    'mem_mask_project': (c_int32, [c_void_p, c_int32, c_int32, c_void_p, c_void_p, c_void_p]),
     'mem_plan_set_timing': (c_int32, [c_void_p, c_int32]),
     'mem_plan_phase_times': (c_int32, [c_void_p, ctypes.POINTER(ctypes.c_float), c_int32]),
     'mem_phase_name': (ctypes.c_char_p, [c_int32]),

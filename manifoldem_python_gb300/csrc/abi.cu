@@ -509,22 +509,41 @@ int execute_impl(mem_plan* plan, const mem_inputs* in, const mem_outputs* out, v
     float* img_all = out->img_all ? out->img_all : xbuf;
     MEM_STEP(kern::rotate(P, *in, xbuf, img_all, pds, img_pd, spec, s));
     MEM_STEP(mark(3));
-    // (a8) F = fft2(imgAll)
+    // (a8) F = fft2(imgAll); (a7, a9) CTF and per-PD sums.  With a volume mask the spectra of
+    // D, of the phase flips and of imgAvgFlip are those of imgAll * msk2 (:344), while the Wiener
+    // average uses fft2(imgAll) (:355-359): its sums come from the unmasked spectra, then the
+    // masked copy (in xbuf; in place when imgAll lives there) replaces them for the rest.
     const float2* twid = at<float2>(ws, L.twid);
-    if (P.smem_fft)
-        MEM_STEP(kern::spectrum_fft(P, P.n_images, img_all, twid, spec, s));
-    else
-        MEM_STEP(exec_fft(P, CUFFT_R2C, P.n_images, NN, specN, img_all, spec, work, s));
+    auto spectrum = [&](const float* images) -> int {
+        if (P.smem_fft) return kern::spectrum_fft(P, P.n_images, images, twid, spec, s);
+        return exec_fft(P, CUFFT_R2C, P.n_images, NN, specN, const_cast<float*>(images), spec,
+                        work, s);
+    };
+    MEM_STEP(spectrum(img_all));
     MEM_STEP(mark(4));
-    // (a7, a9) CTF, per-PD sums, centring vectors, average spectra
     MEM_STEP(kern::qfix(P, *in, qf, s));
     float* partial = at<float>(ws, L.partial);
-    MEM_STEP(kern::pd_sums(P, spec, qf, at<SumItem>(ws, L.sum_items), partial, s));
     float* means = at<float>(ws, L.means);
     float2* avg_spec = at<float2>(ws, L.avg_spec);
     uint32_t* pd_max = at<uint32_t>(ws, L.pd_max);
-    MEM_STEP(kern::pd_finalize(P, partial, at<SumItem>(ws, L.sum_items),
-                               at<int32_t>(ws, L.item_off), pds, means, avg_spec, pd_max, s));
+    const SumItem* items = at<SumItem>(ws, L.sum_items);
+    const int32_t* item_off = at<int32_t>(ws, L.item_off);
+    if (in->pd_mask) {
+        // the Wiener average from the unmasked spectra, then everything else (centring vectors
+        // included, so that they centre the features D is computed from) from the masked ones
+        MEM_STEP(kern::pd_sums(P, spec, qf, items, partial, 1, s));
+        MEM_STEP(kern::pd_finalize(P, partial, items, item_off, pds, means, avg_spec, pd_max, 1,
+                                   s));
+        MEM_STEP(kern::apply_pd_mask(P, img_all, xbuf, in->pd_mask, img_pd, s));
+        MEM_STEP(spectrum(xbuf));
+        MEM_STEP(kern::pd_sums(P, spec, qf, items, partial, 3, s));
+        MEM_STEP(kern::pd_finalize(P, partial, items, item_off, pds, means, avg_spec, pd_max, 2,
+                                   s));
+    } else {
+        MEM_STEP(kern::pd_sums(P, spec, qf, items, partial, 3, s));
+        MEM_STEP(kern::pd_finalize(P, partial, items, item_off, pds, means, avg_spec, pd_max, 3,
+                                   s));
+    }
     MEM_STEP(mark(5));
     // features of D, a_i, sign(C) F, CTF output
     void* feat_a = at<char>(ws, L.feat_a);
@@ -542,7 +561,7 @@ int execute_impl(mem_plan* plan, const mem_inputs* in, const mem_outputs* out, v
             MEM_STEP(kern::inverse_fft(P, 2 * P.n_pd, avg_spec, twid, avg_real, nullptr, false, s));
         else
             MEM_STEP(exec_fft(P, CUFFT_C2R, 2 * P.n_pd, specN, NN, avg_spec, avg_real, work, s));
-        MEM_STEP(kern::avg_store(P, avg_real, out->img_avg, out->img_avg_flip, s));
+        MEM_STEP(kern::avg_store(P, avg_real, out->img_avg, out->img_avg_flip, in->pd_mask, s));
     }
     MEM_STEP(mark(7));
     // phase-flipped images and their mean intensity

@@ -120,6 +120,9 @@ int lowpass_table(const mem_plan& P, float* gtab, cudaStream_t s);
 int lowpass_fused(const mem_plan& P, const mem_inputs& in, const float* gtab,
                   const float2* twid, float* xbuf, uint32_t* status, int64_t max_ctas,
                   cudaStream_t s);
+// dst[img] = src[img] times the mask of the image's PD (in place when dst == src)
+int apply_pd_mask(const mem_plan& P, const float* src, float* dst, const uint8_t* masks,
+                  const int32_t* img_pd, cudaStream_t s);
 // RELION read: shifted images, laid out as SPIDER stack images, into out [n_images][N][N]
 int relion_shift(const mem_plan& P, const mem_inputs& in, float* out, uint32_t* status,
                  cudaStream_t s);
@@ -132,18 +135,20 @@ int inverse_fft(const mem_plan& P, int64_t count, const float2* spec, const floa
 int rotate(const mem_plan& P, const mem_inputs& in, float* xbuf, float* img_out,
            const PdDev* pd_table, const int32_t* img_pd, float2* spec, cudaStream_t s);
 int qfix(const mem_plan& P, const mem_inputs& in, uint64_t* qf, cudaStream_t s);
+// which: 1 = S0..S2, 2 = S3..S5, 3 = all six per-PD sums
 int pd_sums(const mem_plan& P, const float2* spec, const uint64_t* qf, const SumItem* items,
-            float* partial, cudaStream_t s);
+            float* partial, int which, cudaStream_t s);
+// mode bit 1: Wiener average spectrum; bit 2: centring vectors, scale, phase-flip average
 int pd_finalize(const mem_plan& P, const float* partial, const SumItem* items,
                 const int32_t* item_off, const PdDev* pds, float* means, float2* avg_spec,
-                uint32_t* pd_max, cudaStream_t s);
+                uint32_t* pd_max, int mode, cudaStream_t s);
 int features(const mem_plan& P, float2* spec, const uint64_t* qf, const PdDev* pds,
              const int32_t* img_pd, const int32_t* img_row, const int32_t* colmap,
              const float* means, const uint32_t* scale_bits, void* feat_a, void* feat_b,
              double* pair_norm, float* ctf_out, float* spectrum_out, bool write_signed,
              cudaStream_t s);
 int avg_store(const mem_plan& P, const float* avg_real, double* img_avg, double* img_avg_flip,
-              cudaStream_t s);
+              const uint8_t* pd_mask, cudaStream_t s);
 int intensity(const mem_plan& P, const float* flip_imgs, const PdDev* pds, double* out,
               cudaStream_t s);
 

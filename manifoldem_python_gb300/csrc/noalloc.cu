@@ -187,10 +187,10 @@ extern "C" int mem_pd_distances_noalloc(const mem_params* params, int32_t n, con
     float* means = at<float>(ws, L.means);
     double* pair_norm = at<double>(ws, L.pair_norm);
     NA_STEP(kern::qfix(P, in, qf, s));
-    NA_STEP(kern::pd_sums(P, spec, qf, at<SumItem>(ws, L.items), at<float>(ws, L.partial), s));
+    NA_STEP(kern::pd_sums(P, spec, qf, at<SumItem>(ws, L.items), at<float>(ws, L.partial), 3, s));
     NA_STEP(kern::pd_finalize(P, at<float>(ws, L.partial), at<SumItem>(ws, L.items),
                               at<int32_t>(ws, L.item_off), pds, means,
-                              at<float2>(ws, L.avg_spec), pd_max, s));
+                              at<float2>(ws, L.avg_spec), pd_max, 3, s));
     NA_STEP(kern::features(P, spec, qf, pds, at<int32_t>(ws, L.img_pd), at<int32_t>(ws, L.img_row),
                            at<int32_t>(ws, L.colmap), means, scale_bits, at<char>(ws, L.feat_a),
                            at<char>(ws, L.feat_b), pair_norm, nullptr, nullptr, false, s));

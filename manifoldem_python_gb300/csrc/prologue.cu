@@ -606,12 +606,12 @@ __global__ void __launch_bounds__(NT, 2) rotate_fixed_kernel(
         s[b * P + a] = xi[p] * mask_ref(b, a, N);
     }
     __syncthreads();
-    float keep[MAXV];
 #pragma unroll 1
     for (int pass = 0; pass < 2; ++pass) {
         prefilter_fixed<NT, N, 0>(s);
         prefilter_fixed<NT, N, 1>(s);
         fill_halo<NT>(s, N, P);
+        float keep[MAXV];
         int base, stride;
         rotate_once<NT, N>(s, rot[pass], keep, base, stride);
         __syncthreads();
@@ -735,6 +735,8 @@ __device__ __forceinline__ float ctf_eval(int m, uint64_t qf, const CtfConst& cc
 // 4. per-PD sums over images (partial, one item = up to kSumChunk images of one PD)
 //    S0 = sum C^2, S1/S2 = sum C F, S3/S4 = sum sign(C) F, S5 = sum |F|^2
 // ------------------------------------------------------------------------------------------
+// WHICH: 1 = S0..S2 (the Wiener sums), 2 = S3..S5, 3 = all six
+template <int WHICH>
 __global__ void __launch_bounds__(256) pd_sums_kernel(
         const float2* __restrict__ spec, const uint64_t* __restrict__ qfix,
         const SumItem* __restrict__ items, float* __restrict__ partial, int N, int Nh, int64_t Kc,
@@ -750,21 +752,31 @@ __global__ void __launch_bounds__(256) pd_sums_kernel(
         for (int64_t i = it.img_begin; i < it.img_end; ++i) {
             const float2 F = spec[i * Kc + k];
             int sg;
-            const float C = ctf_eval(m, qfix[i], cc, &sg);
-            s0.add(C * C);
-            s1.add(C * F.x);
-            s2.add(C * F.y);
-            s3.add(sg > 0 ? F.x : (sg < 0 ? -F.x : 0.f));
-            s4.add(sg > 0 ? F.y : (sg < 0 ? -F.y : 0.f));
-            s5.add(F.x * F.x + F.y * F.y);
+            if (WHICH & 1) {
+                const float C = ctf_eval(m, qfix[i], cc, &sg);
+                s0.add(C * C);
+                s1.add(C * F.x);
+                s2.add(C * F.y);
+            } else {
+                sg = ctf_sign(m, qfix[i], cc);
+            }
+            if (WHICH & 2) {
+                s3.add(sg > 0 ? F.x : (sg < 0 ? -F.x : 0.f));
+                s4.add(sg > 0 ? F.y : (sg < 0 ? -F.y : 0.f));
+                s5.add(F.x * F.x + F.y * F.y);
+            }
         }
         float* out = partial + (int64_t)blockIdx.x * 6 * Kc + k;
-        out[0 * Kc] = s0.value();
-        out[1 * Kc] = s1.value();
-        out[2 * Kc] = s2.value();
-        out[3 * Kc] = s3.value();
-        out[4 * Kc] = s4.value();
-        out[5 * Kc] = s5.value();
+        if (WHICH & 1) {
+            out[0 * Kc] = s0.value();
+            out[1 * Kc] = s1.value();
+            out[2 * Kc] = s2.value();
+        }
+        if (WHICH & 2) {
+            out[3 * Kc] = s3.value();
+            out[4 * Kc] = s4.value();
+            out[5 * Kc] = s5.value();
+        }
     }
 }
 
@@ -773,12 +785,15 @@ __global__ void __launch_bounds__(256) pd_finalize_kernel(
         const float* __restrict__ partial, const SumItem* __restrict__ items,
         const int32_t* __restrict__ item_off, const PdDev* __restrict__ pds,
         float* __restrict__ means, float2* __restrict__ avg_spec, uint32_t* __restrict__ pd_max,
-        int N, int Nh, int64_t Kc, int64_t Kc_pad, int64_t mstride) {
+        int N, int Nh, int64_t Kc, int64_t Kc_pad, int64_t mstride, int mode) {
+    // mode bit 1: the Wiener average spectrum (from S0..S2); bit 2: centring vectors, scale and
+    // the phase-flipped average spectrum
     const int64_t k = blockIdx.y * 256ll + threadIdx.x;
     const int pd = blockIdx.x;
     if (k >= Kc_pad) return;
     float* mu = means + pd * mstride;
     if (k >= Kc) {
+        if (!(mode & 2)) return;
         mu[k] = mu[Kc_pad + k] = mu[2 * Kc_pad + k] = mu[3 * Kc_pad + k] = 0.f;
         return;
     }
@@ -789,6 +804,14 @@ __global__ void __launch_bounds__(256) pd_finalize_kernel(
         for (int j = 0; j < 6; ++j) S[j] += (double)p[j * Kc];
     }
     const int n = pds[pd].n;
+    const double NN = (double)N * N;
+    float2* av = avg_spec + (int64_t)pd * 2 * Kc;
+    if (mode & 1) {
+        // Wiener average (reference :353-366): sum_i F_i C_i / -(sum C^2 + 1/5), / N^2, / n
+        const double wd = -(S[0] + 0.2);
+        av[k] = make_float2((float)(S[1] / wd / NN / n), (float)(S[2] / wd / NN / n));
+    }
+    if (!(mode & 2)) return;
     const int kb = (int)(k % Nh);
     const double w = (kb == 0 || (N % 2 == 0 && kb == N / 2)) ? 1.0 : 2.0;
     const double sw = sqrt(w), s2w = sqrt(2.0 * w);
@@ -800,11 +823,6 @@ __global__ void __launch_bounds__(256) pd_finalize_kernel(
     mu[3 * Kc_pad + k] = mu_s;
     const float mx = fmaxf(fmaxf(fabsf(mu_u), fabsf(mu_v)), fmaxf(fabsf(mu_r), fabsf(mu_s)));
     atomicMax(pd_max + pd, __float_as_uint(mx));
-    // Wiener average (reference :353-366): sum_i F_i C_i / -(sum C^2 + 1/5), / N^2 (ifft2), / n
-    const double NN = (double)N * N;
-    const double wd = -(S[0] + 0.2);
-    float2* av = avg_spec + (int64_t)pd * 2 * Kc;
-    av[k] = make_float2((float)(S[1] / wd / NN / n), (float)(S[2] / wd / NN / n));
     // phase-flipped average (:346-348, :367): sum_i sign(C_i) F_i / N^2 / n
     av[Kc + k] = make_float2((float)(S[3] / NN / n), (float)(S[4] / NN / n));
 }
@@ -912,13 +930,16 @@ __global__ void __launch_bounds__(256) features_kernel(
 }
 
 // 7. averages: float C2R results -> double outputs (the reference keeps them in float64)
+// with a volume mask both averages are multiplied by the PD's msk2 (reference :366-367)
 __global__ void avg_store_kernel(const float* __restrict__ avg_real, double* __restrict__ img_avg,
-                                 double* __restrict__ img_avg_flip, int64_t n_pd, int NN) {
+                                 double* __restrict__ img_avg_flip, int64_t n_pd, int NN,
+                                 const uint8_t* __restrict__ pd_mask) {
     const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (e >= n_pd * NN) return;
     const int64_t pd = e / NN, p = e - pd * NN;
-    if (img_avg) img_avg[e] = (double)avg_real[(pd * 2) * NN + p];
-    if (img_avg_flip) img_avg_flip[e] = (double)avg_real[(pd * 2 + 1) * NN + p];
+    const bool keep = pd_mask == nullptr || pd_mask[e] != 0;
+    if (img_avg) img_avg[e] = keep ? (double)avg_real[(pd * 2) * NN + p] : 0.0;
+    if (img_avg_flip) img_avg_flip[e] = keep ? (double)avg_real[(pd * 2 + 1) * NN + p] : 0.0;
 }
 
 // 8. imgAllIntensity = mean_i imgAllFlip_i^2 (reference :400)
@@ -1032,22 +1053,27 @@ int qfix(const mem_plan& P, const mem_inputs& in, uint64_t* qf, cudaStream_t s) 
 }
 
 int pd_sums(const mem_plan& P, const float2* spec, const uint64_t* qf, const SumItem* items,
-            float* partial, cudaStream_t s) {
+            float* partial, int which, cudaStream_t s) {
     if (P.items.empty()) return MEM_OK;
     dim3 grid((unsigned)P.items.size(), (unsigned)((P.Kc + 255) / 256));
-    pd_sums_kernel<<<grid, 256, 0, s>>>(spec, qf, items, partial, P.N, P.Nh, P.Kc, P.ctf);
+    if (which == 1)
+        pd_sums_kernel<1><<<grid, 256, 0, s>>>(spec, qf, items, partial, P.N, P.Nh, P.Kc, P.ctf);
+    else if (which == 2)
+        pd_sums_kernel<2><<<grid, 256, 0, s>>>(spec, qf, items, partial, P.N, P.Nh, P.Kc, P.ctf);
+    else
+        pd_sums_kernel<3><<<grid, 256, 0, s>>>(spec, qf, items, partial, P.N, P.Nh, P.Kc, P.ctf);
     MEM_LAUNCH_CHECK();
     return MEM_OK;
 }
 
 int pd_finalize(const mem_plan& P, const float* partial, const SumItem* items,
                 const int32_t* item_off, const PdDev* pds, float* means, float2* avg_spec,
-                uint32_t* pd_max, cudaStream_t s) {
-    MEM_CUDA_TRY(cudaMemsetAsync(pd_max, 0, sizeof(uint32_t) * P.n_pd, s));
+                uint32_t* pd_max, int mode, cudaStream_t s) {
+    if (mode & 2) MEM_CUDA_TRY(cudaMemsetAsync(pd_max, 0, sizeof(uint32_t) * P.n_pd, s));
     dim3 grid((unsigned)P.n_pd, (unsigned)((P.Kc_pad + 255) / 256));
     pd_finalize_kernel<<<grid, 256, 0, s>>>(partial, items, item_off, pds, means, avg_spec,
                                             pd_max, P.N, P.Nh, P.Kc, P.Kc_pad,
-                                            means_stride(P));
+                                            means_stride(P), mode);
     MEM_LAUNCH_CHECK();
     return MEM_OK;
 }
@@ -1073,12 +1099,12 @@ int features(const mem_plan& P, float2* spec, const uint64_t* qf, const PdDev* p
 }
 
 int avg_store(const mem_plan& P, const float* avg_real, double* img_avg, double* img_avg_flip,
-              cudaStream_t s) {
+              const uint8_t* pd_mask, cudaStream_t s) {
     if (!img_avg && !img_avg_flip) return MEM_OK;
     const int NN = P.N * P.N;
     const int64_t total = (int64_t)P.n_pd * NN;
-    avg_store_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(avg_real, img_avg,
-                                                                    img_avg_flip, P.n_pd, NN);
+    avg_store_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(
+            avg_real, img_avg, img_avg_flip, P.n_pd, NN, pd_mask);
     MEM_LAUNCH_CHECK();
     return MEM_OK;
 }

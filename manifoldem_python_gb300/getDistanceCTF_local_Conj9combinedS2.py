@@ -67,6 +67,16 @@ def read_relion_images(imgFileName: str, stack_index: np.ndarray, sh):
     return imgs, inv.astype(np.int64), sh_c
 
 
+def volume_mask(p, device):
+    """The GPU projector of p.mask_vol_file's volume (:303-308), or None without a mask file."""
+    path = getattr(p, 'mask_vol_file', '')
+    if not path:
+        return None
+    from . import mrc
+    from .pipeline import VolumeMask
+    return VolumeMask(np.asarray(mrc.read_stack(path)), device)
+
+
 def load_images(imgFileName: str, stack_index: np.ndarray, N: int, options: dict, sh):
     """The stage's image input for either branch: (images, compact index, shifts or None)."""
     if options.get('relion_data'):
@@ -102,17 +112,16 @@ def op(input_data, filterPar, imgFileName, sh, nStot, options):
     q = np.asarray(q, dtype=np.float64)
     df = np.asarray(df, dtype=np.float64)
     N = int(p.nPix)
-    if getattr(p, 'mask_vol_file', ''):
-        raise NotImplementedError('volume masks (p.mask_vol_file) are not supported by the GPU '
-                                  'stage yet')
     stage = DistanceStage(stage_params(p, filterPar, options))
+    mask = volume_mask(p, stage.device)
     job = PdJob(ind=ind, q=q, df=df, outFile=outFile, prD=prD)
     geom = stage.geometry([job], nStot)[0]
     imgs, compact, sh_c = load_images(imgFileName, geom.stack_index, N, options, sh)
     geom.stack_index = compact
     stack = torch.from_numpy(imgs).to(stage.device)
-    res = stage.run([job], stack, nStot, outputs=DEFAULT_OUTPUTS, geoms=[geom], sh=sh_c)[0]
-    out = assemble(job, geom, res, N, options)
+    res = stage.run([job], stack, nStot, outputs=DEFAULT_OUTPUTS, geoms=[geom], sh=sh_c,
+                    mask=mask)[0]
+    out = assemble(job, geom, res, N, options, msk2=res.get('msk2', 1))
     myio.fout1(outFile, OUTPUT_KEYS, [out[k] for k in OUTPUT_KEYS])
     progress_fname = os.path.join(p.dist_prog, '%s' % prD)
     open(progress_fname, 'a').close()

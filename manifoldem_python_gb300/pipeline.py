@@ -112,16 +112,17 @@ class Plan:
         return out
 
     def execute(self, stack, stack_index, flip, psi_rad, df, outputs: Dict[str, object],
-                stream=None, shift_yx=None) -> None:
+                stream=None, shift_yx=None, pd_mask=None) -> None:
         """Enqueue the stage on ``stream`` (default: torch's current stream).  All tensors
         must be on the plan's device.  ``shift_yx`` ([n_images, 2] float64): a RELION stack,
-        see ``relion_shifts``."""
+        see ``relion_shifts``; ``pd_mask`` ([n_pd, N, N] uint8): volume masks, see
+        ``VolumeMask``."""
         import torch
         stream = stream or torch.cuda.current_stream(self.device)
         cin = _lib.MemInputs(stack=stack.data_ptr(), num_stack=int(stack.shape[0]),
                              stack_index=stack_index.data_ptr(), flip=flip.data_ptr(),
                              psi_rad=psi_rad.data_ptr(), df=df.data_ptr(),
-                             shift_yx=_ptr(shift_yx))
+                             shift_yx=_ptr(shift_yx), pd_mask=_ptr(pd_mask))
         cout = _lib.MemOutputs(**{k: _ptr(outputs.get(k)) for k in OUTPUT_NAMES})
         self._keep = (cin, cout)
         _lib.check(self.lib.mem_plan_execute(self.handle, ctypes.byref(cin), ctypes.byref(cout),
@@ -135,7 +136,8 @@ class Plan:
         ``stream`` (mem_plan_execute_split); ``stack`` may be a pinned host tensor."""
         cin = _lib.MemInputs(stack=stack.data_ptr(), num_stack=int(stack.shape[0]),
                              stack_index=stack_index.data_ptr(), flip=flip.data_ptr(),
-                             psi_rad=psi_rad.data_ptr(), df=df.data_ptr(), shift_yx=None)
+                             psi_rad=psi_rad.data_ptr(), df=df.data_ptr(), shift_yx=None,
+                             pd_mask=None)
         cout = _lib.MemOutputs(**{k: _ptr(outputs.get(k)) for k in OUTPUT_NAMES})
         self._keep = (cin, cout)
         _lib.check(self.lib.mem_plan_execute_split(
@@ -226,10 +228,13 @@ class DistanceStage:
                 for j in jobs]
 
     def run(self, jobs: Sequence[PdJob], stack, nStot: int, outputs=DEFAULT_OUTPUTS,
-            geoms: Optional[Sequence[PdGeometry]] = None, to_host: bool = True, sh=None):
+            geoms: Optional[Sequence[PdGeometry]] = None, to_host: bool = True, sh=None,
+            mask: Optional['VolumeMask'] = None):
         """Run every job; returns one dict per PD with host numpy (``to_host``) or device
         arrays.  ``stack`` is a device tensor (num_part, N, N) float32 in SPIDER storage order,
-        or, with ``sh`` = (shx, shy) per particle, the images of a RELION stack as stored."""
+        or, with ``sh`` = (shx, shy) per particle, the images of a RELION stack as stored.
+        With a volume ``mask`` every PD's projected mask multiplies its spectra and averages
+        and is returned as ``msk2`` (N x N bool)."""
         import torch
         geoms = list(geoms) if geoms is not None else self.geometry(jobs, nStot)
         counts = [int(np.asarray(j.ind).shape[0]) for j in jobs]
@@ -245,10 +250,58 @@ class DistanceStage:
         if sh is not None:
             shifts = torch.from_numpy(relion_shifts(
                 np.concatenate([g.stack_index for g in geoms]), sh)).to(dev)
-        plan.execute(stack, sidx, flip, psi, df, outs, shift_yx=shifts)
+        masks = mask.project(geoms) if mask is not None else None
+        plan.execute(stack, sidx, flip, psi, df, outs, shift_yx=shifts, pd_mask=masks)
         torch.cuda.synchronize(dev)
         plan.device_status()
-        return split_outputs(plan, counts, outs, to_host)
+        res = split_outputs(plan, counts, outs, to_host)
+        if masks is not None:
+            for r, m in zip(res, masks.bool()):
+                r['msk2'] = m.cpu().numpy() if to_host else m
+        return res
+
+
+class VolumeMask:
+    """projectMask.op (modules/projectMask.py:118-135) on the GPU for one mask volume: the
+    spline coefficients are prepared once (mem_mask_prepare), the mask of each PD is projected
+    with the PD's affine map (mem_mask_project, geometry.mask_transform)."""
+
+    def __init__(self, volume, device=None):
+        import torch
+        self.lib = _lib.load()
+        self.device = torch.device(device or 'cuda')
+        vol = np.ascontiguousarray(volume, dtype=np.float32)
+        if vol.ndim != 3 or not (vol.shape[0] == vol.shape[1] == vol.shape[2]):
+            raise ValueError('the mask volume must be an N x N x N cube')
+        self.N = int(vol.shape[0])
+        size = ctypes.c_size_t()
+        _lib.check(self.lib.mem_mask_coefficients_size(self.N, ctypes.byref(size)),
+                   'mask size')
+        v = torch.from_numpy(vol).to(self.device)
+        self.coeffs = torch.empty(size.value // 8, dtype=torch.float64, device=self.device)
+        stream = torch.cuda.current_stream(self.device)
+        _lib.check(self.lib.mem_mask_prepare(v.data_ptr(), self.N, self.coeffs.data_ptr(),
+                                             ctypes.c_void_p(stream.cuda_stream)),
+                   'mem_mask_prepare')
+        torch.cuda.synchronize(self.device)
+
+    def project(self, geoms: Sequence[PdGeometry]):
+        """uint8 (n_pd, N, N) device tensor of 0/1 masks, one per PD geometry."""
+        import torch
+        from .geometry import mask_transform
+        xf = np.empty((len(geoms), 12), dtype=np.float64)
+        for i, g in enumerate(geoms):
+            R, off = mask_transform(np.asarray(g.PD, dtype=np.float64).reshape(-1), self.N)
+            xf[i, :9] = R.reshape(-1)
+            xf[i, 9:] = off
+        xf_d = torch.from_numpy(xf).to(self.device)
+        out = torch.empty((len(geoms), self.N, self.N), dtype=torch.uint8, device=self.device)
+        stream = torch.cuda.current_stream(self.device)
+        _lib.check(self.lib.mem_mask_project(self.coeffs.data_ptr(), self.N, len(geoms),
+                                             xf_d.data_ptr(), out.data_ptr(),
+                                             ctypes.c_void_p(stream.cuda_stream)),
+                   'mem_mask_project')
+        return out
 
 
 def relion_shifts(stack_index: np.ndarray, sh) -> np.ndarray:

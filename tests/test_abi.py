@@ -37,7 +37,7 @@ def test_exports_every_declared_symbol(lib):
 
 def test_struct_layouts_match_header():
     assert ctypes.sizeof(_lib.MemParams) == 72
-    assert ctypes.sizeof(_lib.MemInputs) == 56
+    assert ctypes.sizeof(_lib.MemInputs) == 64
     assert ctypes.sizeof(_lib.MemOutputs) == 72
 
 

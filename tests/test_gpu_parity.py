@@ -14,8 +14,8 @@ import tempfile
 import numpy as np
 import pytest
 
-from conftest import (GOLDEN_CASES, golden_micro, golden_options, golden_ref, golden_shifts,
-                      load_golden)
+from conftest import (GOLDEN_CASES, golden_mask_volume, golden_micro, golden_options,
+                      golden_ref, golden_shifts, load_golden)
 
 pytestmark = pytest.mark.gpu
 
@@ -36,7 +36,11 @@ def run_case(torch, g, precision, outputs=None):
     stack = torch.from_numpy(g['stack16'].astype(np.float32)).cuda()
     outs = outputs or ('D', 'img_avg', 'img_avg_flip', 'img_all_intensity', 'img_all',
                        'img_all_flip', 'ctf', 'spectrum')
-    return stage.run([job], stack, int(g['nStot']), outputs=outs, sh=golden_shifts(g))[0]
+    from manifoldem_python_gb300.pipeline import VolumeMask
+    vol = golden_mask_volume(g)
+    mask = VolumeMask(vol) if vol is not None else None
+    return stage.run([job], stack, int(g['nStot']), outputs=outs, sh=golden_shifts(g),
+                     mask=mask)[0]
 
 
 @pytest.mark.parametrize('precision', PRECISIONS)
@@ -60,6 +64,8 @@ def test_stage_matches_reference(cuda_ready, case, precision):
         assert 'D' not in res
         return
     D = res['D']
+    if golden_mask_volume(g) is not None:       # projectMask on the GPU, exact
+        np.testing.assert_array_equal(res['msk2'], g['ref_msk2'])
     Dref = g['ref_D']
     assert rel(D, Dref) < 1e-5, (case, rel(D, Dref))
     np.testing.assert_array_equal(D, D.T)
