@@ -225,6 +225,14 @@ def choose_sample(counts, cores, max_n):
 
 
 # ------------------------------------------------------------------------------- GPU side
+def workload_string(config_name, cfg, counts):
+    """The workload named in `config` (the same for the GPU arm and the reference arm)."""
+    counts = np.asarray(counts, dtype=np.int64)
+    return '%s: %d PDs, %dx%d px, n~lognormal(median %d), %d images, %d pairs per GPU' % (
+        config_name, len(counts), cfg.N, cfg.N, cfg.n_median, int(counts.sum()),
+        int((counts * (counts - 1) // 2).sum()))
+
+
 def kernels_per_execute(outputs, avg_only, N):
     """Kernels of this library one mem_plan_execute launches (cuFFT kernels excluded).
     N = 32, 64, 128 (shared-memory FFTs): lowpass_table, lowpass_fft, rotate, spectrum_fft,
@@ -524,7 +532,7 @@ def main():
                     help='streamed: stack left in pinned host memory, PD groups pipelined over '
                          'load / compute / copy streams; copy: one host-to-device copy of the '
                          'stack, then one execute')
-    ap.add_argument('--e2e-groups', type=int, default=4)
+    ap.add_argument('--e2e-groups', type=int, default=8)
     ap.add_argument('--no-dm', action='store_true',
                     help='skip the diffusion-map embedding of a sample of PDs (GPU vs CPU port)')
     ap.add_argument('--dm-pds', type=int, default=8)
@@ -579,8 +587,7 @@ def main():
                     warmup=args.warmup, ms_per_step=float(np.median(walls)) * 1000,
                     higher_is_better=True, scaling='weak', vs_baseline=None, dtype='f64',
                     data='synthetic', impl='reference',
-                    config=dict(workload='%s: %d PDs, %dx%d px' % (args.config, len(counts),
-                                                                  cfg.N, cfg.N)),
+                    config=dict(workload=workload_string(args.config, cfg, counts)),
                     cpu_baseline=dict(value=v, unit='pairs/s', cores=cores, kind='port',
                                       sample=sample),
                     e2e=dict(value=v, unit='pairs/s', h2d_bytes_per_step=0,
@@ -605,9 +612,7 @@ def main():
         warmup=args.warmup, ms_per_step=r['ms'], higher_is_better=True, scaling='weak',
         vs_baseline=None, dtype={'fp32': 'f32', 'bf16x3': 'bf16x3+f32acc'}[args.precision],
         data='synthetic (seeded generator, 3-D Gaussian-blob volume, CTF, SNR %.2g)' % cfg.snr,
-        config=dict(workload='%s: %d PDs, %dx%d px, n~lognormal(median %d), %d images, '
-                             '%d pairs per GPU' % (args.config, len(r['counts']), cfg.N, cfg.N,
-                                                   cfg.n_median, r['n_images'], r['pairs']),
+        config=dict(workload=workload_string(args.config, cfg, r['counts']),
                     precision=args.precision, outputs=list(r['outputs']),
                     l2=('L2 flushed before every timed step (%.2f GB image stack)'
                         if r['l2_flush'] else 'inputs larger than L2 (%.1f GB image stack)') % (

@@ -140,12 +140,13 @@ int mem_plan_upload(mem_plan* plan, void* workspace, size_t workspace_bytes, voi
 int mem_plan_execute(mem_plan* plan, const mem_inputs* in, const mem_outputs* out,
                      void* workspace, size_t workspace_bytes, void* stream);
 
-/* mem_plan_execute with the one kernel that reads the stack (gather + normalisation, fused with
- * the low-pass for N = 32, 64, 128) issued on load_stream and the rest of the stage on stream,
- * which waits for it (an event owned by the plan).  With the stack in host memory the load
- * kernel runs on a small grid (128 CTAs; MEM_HOST_LOAD_CTAS) at the host link's rate, so the
- * loads of one plan overlap the computation of other plans on other streams.  The reference has
- * no counterpart (its workers read the stack from disk, :255-283).  Not for graph capture.  */
+/* mem_plan_execute with the reading of the stack issued on load_stream and the rest of the stage
+ * on stream, which waits for it (an event owned by the plan).  With the stack in host memory
+ * the load stream only copies the entries' images over the host link into free workspace
+ * slots (128 light CTAs without shared memory; MEM_HOST_LOAD_CTAS), so the loads of one plan
+ * overlap the computation of other plans on other streams; a device-resident stack is read by
+ * the first kernel of the stage on load_stream.  The reference has no counterpart (its workers
+ * read the stack from disk, :255-283).  Not for graph capture.                              */
 int mem_plan_execute_split(mem_plan* plan, const mem_inputs* in, const mem_outputs* out,
                            void* workspace, size_t workspace_bytes, void* load_stream,
                            void* stream);

@@ -437,9 +437,10 @@ int execute_impl(mem_plan* plan, const mem_inputs* in, const mem_outputs* out, v
     const mem_plan& P = *plan;
     const Layout& L = P.lay;
     const bool split = ls != s;
-    // the stack-reading kernel of a split execute: a small grid when the stack is host memory,
-    // so that the rest of the GPU keeps computing while it waits on the host link
-    const int64_t load_ctas = (split && is_host_memory(in->stack)) ? P.host_load_ctas : 0;
+    // a split execute with the stack in host memory: the load stream only copies the entries'
+    // images over the host link (a few light CTAs, so the rest of the GPU keeps computing), and
+    // all the arithmetic runs on the copies on the main stream
+    const bool host_copy = split && is_host_memory(in->stack);
     void* ws = workspace;
     uint32_t* status = at<uint32_t>(ws, L.status);
     mem_plan& PM = *plan;
@@ -473,31 +474,47 @@ int execute_impl(mem_plan* plan, const mem_inputs* in, const mem_outputs* out, v
     MEM_STEP(mark(0));
     MEM_STEP(kern::lowpass_table(P, at<float>(ws, L.gtab), ls));
     mem_inputs lin = *in;
+    const int64_t* ident = at<int64_t>(ws, L.ident);
+    cudaStream_t cs = ls;                                // stream of the image arithmetic
+    auto join = [&]() -> int {                           // the main stream waits for the loads
+        if (!split) return MEM_OK;
+        if (!PM.load_done)
+            MEM_CUDA_TRY(cudaEventCreateWithFlags(&PM.load_done, cudaEventDisableTiming));
+        MEM_CUDA_TRY(cudaEventRecord(PM.load_done, ls));
+        MEM_CUDA_TRY(cudaStreamWaitEvent(s, PM.load_done, 0));
+        return MEM_OK;
+    };
+    if (host_copy) {
+        // raw copies into free slots: xbuf when the RELION shift writes the spectrum slots,
+        // the spectrum slots otherwise
+        float* staging = in->shift_yx ? xbuf : reinterpret_cast<float*>(spec);
+        MEM_STEP(kern::gather_copy(P, *in, staging, status, P.host_load_ctas, ls));
+        MEM_STEP(join());
+        cs = s;
+        lin.stack = staging;
+        lin.num_stack = P.n_images;
+        lin.stack_index = ident;
+    }
     if (in->shift_yx) {
         // RELION: shifted copies, laid out as SPIDER images, in the (still free) spectrum
         // slots; the gather then reads copy i for entry i
         float* shifted = reinterpret_cast<float*>(spec);
-        MEM_STEP(kern::relion_shift(P, *in, shifted, status, ls));
+        MEM_STEP(kern::relion_shift(P, lin, shifted, status, cs));
         lin.stack = shifted;
         lin.num_stack = P.n_images;
-        lin.stack_index = at<int64_t>(ws, L.ident);
+        lin.stack_index = ident;
     }
     if (P.smem_fft) {
         // (a2, a3) gather, flip, normalisation and low-pass in one shared-memory pass
         MEM_STEP(mark(1));
         MEM_STEP(kern::lowpass_fused(P, lin, at<float>(ws, L.gtab), at<float2>(ws, L.twid), xbuf,
-                                     status, in->shift_yx ? 0 : load_ctas, ls));
+                                     status, cs));
     } else {
         // (a2) gather, conjugate flip, normalisation
-        MEM_STEP(kern::gather_normalize(P, lin, xbuf, status, in->shift_yx ? 0 : load_ctas, ls));
+        MEM_STEP(kern::gather_normalize(P, lin, xbuf, status, 0, cs));
         MEM_STEP(mark(1));
     }
-    if (split) {
-        if (!PM.load_done)
-            MEM_CUDA_TRY(cudaEventCreateWithFlags(&PM.load_done, cudaEventDisableTiming));
-        MEM_CUDA_TRY(cudaEventRecord(PM.load_done, ls));
-        MEM_CUDA_TRY(cudaStreamWaitEvent(s, PM.load_done, 0));
-    }
+    if (!host_copy) MEM_STEP(join());
     if (!P.smem_fft) {
         // (a3) low-pass filter: R2C, multiply by G/N^2, C2R
         MEM_STEP(exec_fft(P, CUFFT_R2C, P.n_images, NN, specN, xbuf, spec, work, s));

@@ -28,8 +28,6 @@
 // owns 8 pair-rows and 8 columns, so only the row<->column hand-overs need a block barrier.
 // The position swizzle makes every shared-memory access of the four pass shapes conflict-free
 // for N = 128.
-#include <algorithm>
-
 #include "fft_radix.cuh"
 #include "mem_internal.cuh"
 
@@ -476,28 +474,18 @@ __device__ __forceinline__ void lowpass_image(
     F::rows_inverse(S, W, dst);
 }
 
-// one image per CTA, or (LOOP) a grid smaller than the batch looping over the images: a stack
-// in host memory is then read at the host link's rate by a few SMs while the rest of the GPU
-// computes
-template <int N, bool LOOP>
+// one image per CTA
+template <int N>
 __global__ void __launch_bounds__(2 * N, N == 128 ? 2 : 4) lowpass_fft_kernel(
         const float* __restrict__ stack, int64_t num_stack, const int64_t* __restrict__ sidx,
         const uint8_t* __restrict__ flip, const float* __restrict__ gtab,
-        const float2* __restrict__ twid, float* __restrict__ xbuf, uint32_t* __restrict__ status,
-        int64_t n_images) {
+        const float2* __restrict__ twid, float* __restrict__ xbuf, uint32_t* __restrict__ status) {
     using F = Fft2<N>;
     extern __shared__ float2 S[];                      // [N/2][N], swizzled
     __shared__ float2 W[N];
     __shared__ double red[F::NT / 32];
     F::twiddles(W, twid);
-    if constexpr (!LOOP) {
-        lowpass_image<N>(blockIdx.x, S, W, red, stack, num_stack, sidx, flip, gtab, xbuf, status);
-    } else {
-        for (int64_t img = blockIdx.x; img < n_images; img += gridDim.x) {
-            __syncthreads();                           // S and red free from the last image
-            lowpass_image<N>(img, S, W, red, stack, num_stack, sidx, flip, gtab, xbuf, status);
-        }
-    }
+    lowpass_image<N>(blockIdx.x, S, W, red, stack, num_stack, sidx, flip, gtab, xbuf, status);
 }
 
 template <int N>
@@ -557,24 +545,14 @@ bool smem_fft_supported(const mem_plan& P) { return P.N == 32 || P.N == 64 || P.
     }
 
 int lowpass_fused(const mem_plan& P, const mem_inputs& in, const float* gtab,
-                  const float2* twid, float* xbuf, uint32_t* status, int64_t max_ctas,
-                  cudaStream_t s) {
+                  const float2* twid, float* xbuf, uint32_t* status, cudaStream_t s) {
     if (P.n_images == 0) return MEM_OK;
     const size_t smem = (size_t)(P.N / 2) * P.N * sizeof(float2);
-    const int64_t grid = max_ctas > 0 ? std::min<int64_t>(max_ctas, P.n_images) : P.n_images;
 #define MEM_CALL(NV)                                                                           \
     do {                                                                                       \
-        if (grid < P.n_images) {                                                               \
-            if (prepare(lowpass_fft_kernel<NV, true>, smem) != MEM_OK) return MEM_ERR_CUDA;    \
-            lowpass_fft_kernel<NV, true><<<(unsigned)grid, 2 * NV, smem, s>>>(                 \
-                    in.stack, in.num_stack, in.stack_index, in.flip, gtab, twid, xbuf, status, \
-                    P.n_images);                                                               \
-        } else {                                                                               \
-            if (prepare(lowpass_fft_kernel<NV, false>, smem) != MEM_OK) return MEM_ERR_CUDA;   \
-            lowpass_fft_kernel<NV, false><<<(unsigned)grid, 2 * NV, smem, s>>>(                \
-                    in.stack, in.num_stack, in.stack_index, in.flip, gtab, twid, xbuf, status, \
-                    P.n_images);                                                               \
-        }                                                                                      \
+        if (prepare(lowpass_fft_kernel<NV>, smem) != MEM_OK) return MEM_ERR_CUDA;              \
+        lowpass_fft_kernel<NV><<<(unsigned)P.n_images, 2 * NV, smem, s>>>(                     \
+                in.stack, in.num_stack, in.stack_index, in.flip, gtab, twid, xbuf, status);    \
     } while (0)
     MEM_FFT_DISPATCH(MEM_CALL)
 #undef MEM_CALL

@@ -92,8 +92,8 @@ struct mem_plan {
     bool tc_kahan = false;          // compensated register sums across groups
     bool tc_lolo = false;           // add the lo.lo product (4-term split)
     bool smem_fft = true;           // shared-memory FFT kernels instead of cuFFT (N = 32, 64, 128)
-    int host_load_ctas = 128;       // grid of the stack-reading kernel when the stack is in host
-                                    // memory and the load runs on its own stream
+    int host_load_ctas = 128;       // grid of the host-to-device image copy of a split execute
+                                    // with the stack in host memory
     bool timing = false;
     bool timed_run = false;
     cudaEvent_t ev[MEM_NUM_PHASES + 1] = {};
@@ -112,14 +112,15 @@ namespace mem {
 namespace kern {
 int gather_normalize(const mem_plan& P, const mem_inputs& in, float* xbuf, uint32_t* status,
                      int64_t max_ctas, cudaStream_t s);
+// raw copies of the entries' stack images into out [n_images][N][N] (ctas CTAs loop over them)
+int gather_copy(const mem_plan& P, const mem_inputs& in, float* out, uint32_t* status,
+                int64_t ctas, cudaStream_t s);
 // multiply the half-plane spectra by the table G/N^2 written by lowpass_table
 int lowpass(const mem_plan& P, float2* spec, float* gtab, cudaStream_t s);
 bool smem_fft_supported(const mem_plan& P);
 int lowpass_table(const mem_plan& P, float* gtab, cudaStream_t s);
-// max_ctas > 0: a grid of at most max_ctas CTAs loops over the images
 int lowpass_fused(const mem_plan& P, const mem_inputs& in, const float* gtab,
-                  const float2* twid, float* xbuf, uint32_t* status, int64_t max_ctas,
-                  cudaStream_t s);
+                  const float2* twid, float* xbuf, uint32_t* status, cudaStream_t s);
 // dst[img] = src[img] times the mask of the image's PD (in place when dst == src)
 int apply_pd_mask(const mem_plan& P, const float* src, float* dst, const uint8_t* masks,
                   const int32_t* img_pd, cudaStream_t s);

@@ -112,6 +112,32 @@ __global__ void __launch_bounds__(NT) gather_normalize_kernel(
     }
 }
 
+// raw copy of every entry's stack image into slot i of out (a stack in host memory read over
+// the host link by a few light CTAs; the arithmetic then runs on the copies)
+__global__ void __launch_bounds__(256) gather_copy_kernel(
+        const float* __restrict__ stack, int64_t num_stack, const int64_t* __restrict__ sidx,
+        int64_t n_images, int NN, float* __restrict__ out, uint32_t* __restrict__ status) {
+    for (int64_t img = blockIdx.x; img < n_images; img += gridDim.x) {
+        const int64_t s = sidx[img];
+        float* dst = out + img * (int64_t)NN;
+        if (s < 0 || s >= num_stack) {
+            if (threadIdx.x == 0) atomicOr(status, 2u);
+            for (int p = threadIdx.x; p < NN; p += blockDim.x) dst[p] = __int_as_float(0x7fc00000);
+            continue;
+        }
+        const float* src = stack + s * (int64_t)NN;
+        if ((NN & 3) == 0) {
+            const float4* s4 = reinterpret_cast<const float4*>(src);
+            float4* d4 = reinterpret_cast<float4*>(dst);
+#pragma unroll 8
+            for (int p = threadIdx.x; p < NN / 4; p += blockDim.x) d4[p] = s4[p];
+        } else {
+#pragma unroll 8
+            for (int p = threadIdx.x; p < NN; p += blockDim.x) dst[p] = src[p];
+        }
+    }
+}
+
 // float4 variant for N % 4 == 0: one 16-byte load / store per 4 pixels of a stack row; a
 // conjugate flip reverses the four lanes (the row reversal maps aligned quads to aligned quads)
 template <int NT>
@@ -975,6 +1001,16 @@ int gather_normalize(const mem_plan& P, const mem_inputs& in, float* xbuf, uint3
     else
         gather_normalize_kernel<256><<<(unsigned)grid, 256, 0, s>>>(
             in.stack, in.num_stack, in.stack_index, in.flip, xbuf, P.N, status, P.n_images);
+    MEM_LAUNCH_CHECK();
+    return MEM_OK;
+}
+
+int gather_copy(const mem_plan& P, const mem_inputs& in, float* out, uint32_t* status,
+                int64_t ctas, cudaStream_t s) {
+    if (P.n_images == 0) return MEM_OK;
+    const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(ctas, P.n_images));
+    gather_copy_kernel<<<(unsigned)grid, 256, 0, s>>>(in.stack, in.num_stack, in.stack_index,
+                                                      P.n_images, P.N * P.N, out, status);
     MEM_LAUNCH_CHECK();
     return MEM_OK;
 }
