@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define MEM_ABI_VERSION 3
+#define MEM_ABI_VERSION 4
 
 /* status codes */
 #define MEM_OK                    0
@@ -232,6 +232,31 @@ int mem_mask_coefficients_size(int32_t N, size_t* bytes);
 int mem_mask_prepare(const float* volume, int32_t N, double* coeffs, void* stream);
 int mem_mask_project(const double* coeffs, int32_t N, int32_t n_pd, const double* transforms,
                      uint8_t* masks, void* stream);
+
+/* ---- NLSA snapshot stage (reference modules/NLSA.py:23-158, get_wiener.py:9-21) ------------
+ * The per-PD arrays of NLSA.op that scale with the images; the caller keeps the two embeddings,
+ * the small SVD and the curve fit (as manifoldem_python_gb300/NLSA.py does).  Device pointers,
+ * row-major.  num = images in the PD, c = ConOrder (1 <= c < num), m = num - c.
+ *
+ * mem_nlsa_con_distances: ConD (m x m f64) = sum_{i < c} DD[i:i+m, i:i+m] (DD num x num f64),
+ *   added in order i = 0, 1, .. from 0 (NLSA.py:31-34): bit-identical to the reference.
+ * mem_nlsa_snapshots: A (c N^2 x n_modes f64) of NLSA.py:63-86, block ii (rows ii N^2 ..) =
+ *   tmp_ii mu_psi with column i of tmp_ii the snapshot j = c - ii + i - 1 transposed and
+ *   flattened (row x N + y holds pixel [y][x]):
+ *     ctf != NULL (the 'prD' branch): snapshot = msk2 * Re ifft2(fft2(images[j]) ctf[j] / wd_i),
+ *       wd_i = sum_{t = i+1 .. i+c} ctf[t]^2 + 1/5 (get_wiener.py), msk2 (N x N f64) or NULL
+ *       for 1.  ctf[j] must be even in frequency, as every CTF of the distance stage is
+ *       (C(-k) = C(k) on the ifftshifted grid); the Wiener sum runs over half-plane spectra.
+ *     ctf == NULL (the 'cuti' branch): snapshot = images[j], no filter and no mask.
+ *   images, ctf: (num, N, N) float32 as stored (ctf ifftshifted); mu_psi: m x n_modes f64.
+ *   Spectra and the banded Wiener sum in float32 with float64 Wiener denominators; A float64.
+ *   workspace: mem_nlsa_workspace_size bytes.  N <= 512, 1 <= n_modes <= 64.                */
+int mem_nlsa_con_distances(const double* DD, int32_t num, int32_t c, double* ConD, void* stream);
+int mem_nlsa_workspace_size(int32_t N, int32_t num, int32_t c, int32_t n_modes, int32_t wiener,
+                            size_t* bytes);
+int mem_nlsa_snapshots(int32_t N, int32_t num, int32_t c, int32_t n_modes, const float* images,
+                       const float* ctf, const double* mu_psi, const double* msk2,
+                       void* workspace, size_t workspace_bytes, double* A, void* stream);
 
 #ifdef __cplusplus
 }

@@ -22,7 +22,7 @@ INCLUDE = os.path.join(REPO, 'include')
 BUILD_DIR = os.path.join(REPO, '_build')
 LIB_PATH = os.path.join(HERE, 'libmanifoldem_gb300.so')
 SOURCES = ['abi.cu', 'prologue.cu', 'gemm_fp32.cu', 'gemm_tc.cu', 'noalloc.cu', 'image_fft.cu',
-           'dmap.cu', 'relion.cu', 'mask.cu']
+           'dmap.cu', 'relion.cu', 'mask.cu', 'nlsa.cu']
 ARCH_FLAGS = ['-gencode', 'arch=compute_103a,code=sm_103a']
 
 # status codes (include/manifoldem_gb300.h)
@@ -112,7 +112,7 @@ class MemParams(ctypes.Structure):
                 ('avg_only', c_int32), ('precision', c_int32)]
 
 
-ABI_VERSION = 3            # MEM_ABI_VERSION of include/manifoldem_gb300.h these structs follow
+ABI_VERSION = 4            # MEM_ABI_VERSION of include/manifoldem_gb300.h these structs follow
 
 
 class MemInputs(ctypes.Structure):
@@ -153,6 +153,12 @@ SIGNATURES = {
     'mem_mask_coefficients_size': (c_int32, [c_int32, ctypes.POINTER(c_size_t)]),
     'mem_mask_prepare': (c_int32, [c_void_p, c_int32, c_void_p, c_void_p]),
     'mem_mask_project': (c_int32, [c_void_p, c_int32, c_int32, c_void_p, c_void_p, c_void_p]),
+    'mem_nlsa_con_distances': (c_int32, [c_void_p, c_int32, c_int32, c_void_p, c_void_p]),
+    'mem_nlsa_workspace_size': (c_int32, [c_int32, c_int32, c_int32, c_int32, c_int32,
+                                          ctypes.POINTER(c_size_t)]),
+    'mem_nlsa_snapshots': (c_int32, [c_int32, c_int32, c_int32, c_int32, c_void_p, c_void_p,
+                                     c_void_p, c_void_p, c_void_p, c_size_t, c_void_p,
+                                     c_void_p]),
     'mem_plan_set_timing': (c_int32, [c_void_p, c_int32]),
     'mem_plan_phase_times': (c_int32, [c_void_p, ctypes.POINTER(ctypes.c_float), c_int32]),
     'mem_phase_name': (ctypes.c_char_p, [c_int32]),

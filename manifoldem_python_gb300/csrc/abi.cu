@@ -70,12 +70,22 @@ void fft_batches(int64_t count, std::vector<int>* batches) {
     if (count % kFftChunk) batches->push_back((int)(count % kFftChunk));
 }
 
-int exec_fft(const mem_plan& P, cufftType type, int64_t count, int64_t in_stride,
+}  // namespace
+
+size_t fft_work_bytes(int N, cufftType type, int64_t count) {
+    std::vector<int> batches;
+    fft_batches(count, &batches);
+    size_t work = 0;
+    for (int b : batches) work = std::max(work, fft_work_estimate(N, type, b));
+    return work;
+}
+
+int fft_exec(int device, int N, cufftType type, int64_t count, int64_t in_stride,
              int64_t out_stride, void* in, void* out, void* work, cudaStream_t s) {
     for (int64_t b = 0; b < count; b += kFftChunk) {
         const int batch = (int)std::min<int64_t>(kFftChunk, count - b);
         FftPlan fp;
-        int st = fft_plan(P.device, P.N, type, batch, &fp);
+        int st = fft_plan(device, N, type, batch, &fp);
         if (st != MEM_OK) return st;
         if (cufftSetStream(fp.h, s) != CUFFT_SUCCESS) return MEM_ERR_CUFFT;
         if (cufftSetWorkArea(fp.h, work) != CUFFT_SUCCESS) return MEM_ERR_CUFFT;
@@ -89,6 +99,13 @@ int exec_fft(const mem_plan& P, cufftType type, int64_t count, int64_t in_stride
         if (r != CUFFT_SUCCESS) return MEM_ERR_CUFFT;
     }
     return MEM_OK;
+}
+
+namespace {
+
+int exec_fft(const mem_plan& P, cufftType type, int64_t count, int64_t in_stride,
+             int64_t out_stride, void* in, void* out, void* work, cudaStream_t s) {
+    return fft_exec(P.device, P.N, type, count, in_stride, out_stride, in, out, work, s);
 }
 
 template <class T>

@@ -108,6 +108,13 @@ struct mem_plan {
 
 namespace mem {
 
+// ---- batched 2D cuFFT transforms of N x N images (abi.cu): R2C image -> half-plane [N][N/2+1]
+// or C2R back, `count` transforms in chunks of kFftChunk from a per-(device, N, kind, batch) plan
+// cache; work is a caller-owned area of fft_work_bytes(N, type, count) bytes
+size_t fft_work_bytes(int N, cufftType type, int64_t count);
+int fft_exec(int device, int N, cufftType type, int64_t count, int64_t in_stride,
+             int64_t out_stride, void* in, void* out, void* work, cudaStream_t s);
+
 // ---- host launchers of the image-side kernels (prologue.cu) ------------------------------
 namespace kern {
 int gather_normalize(const mem_plan& P, const mem_inputs& in, float* xbuf, uint32_t* status,

@@ -61,9 +61,13 @@ def neighbour_lists(D: np.ndarray, k: int):
     return rows.reshape(-1), order.reshape(-1), vals.reshape(-1)
 
 
-def dm_embedding(D: np.ndarray, k: int = None, tune: float = 3, seed: int = 0):
-    """Returns (lambda, psi, sigma) as DMembeddingII.op does (psi = v[:,1:]/v[:,0])."""
-    np.random.seed(seed)
+def dm_embedding(D: np.ndarray, k: int = None, tune: float = 3, seed: int = 0,
+                 full: bool = False):
+    """Returns (lambda, psi, sigma) as DMembeddingII.op does (psi = v[:,1:]/v[:,0]); with
+    ``full`` also the Riemannian measure mu = v[:,0]^2 (DMembeddingII.py:178-181).  ``seed`` None
+    draws from np.random as it stands (a caller that seeded it once for several embeddings)."""
+    if seed is not None:
+        np.random.seed(seed)
     nS = D.shape[0]
     k = nS if k is None else k
     rows, cols, vals = neighbour_lists(D, k)
@@ -101,6 +105,8 @@ def dm_embedding(D: np.ndarray, k: int = None, tune: float = 3, seed: int = 0):
     psi = np.zeros((nS, n_eigs))
     m = vecs.shape[1] - 1
     psi[:, :m] = vecs[:, 1:] / vecs[:, :1]
+    if full:
+        return vals_e, psi, sigma, vecs[:, 0] * vecs[:, 0]
     return vals_e, psi, sigma
 
 

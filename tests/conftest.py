@@ -65,3 +65,54 @@ def cuda_ready():
     _lib.build()
     _lib.load()
     return torch
+
+
+# ---- NLSA fixtures (tests/golden/nlsa32.npz, made by make_golden.py from the reference) -------
+
+NLSA_RUNS = {'a': 'prD', 'b': 'prD-mask', 'c': 'cuti'}
+
+
+def nlsa_golden_args(g, tag):
+    """Arguments of NLSA.op for run `tag` of an NLSA fixture, as psiAnalysisParS2.op builds them
+    (psiAnalysisParS2.py:57-96): all images on the path, ordered along diffusion coordinate 0."""
+    D = g['D']
+    nS = D.shape[0]
+    c = int(g['ConOrder'])
+    P = g['PosPsi1']
+    par = dict(num=nS, ConOrder=c, k=nS - c, tune=3, nS=nS, save=False, psiTrunc=8)
+    msk2 = g['msk_disc'] if tag == 'b' else np.array(1)
+    ext = dict(cuti=0) if tag == 'c' else dict(outDir='', prD=0)
+    return (par, D[P][:, P], np.arange(nS), P, g['imgAll'].astype(np.float64), msk2,
+            g['CTF'].astype(np.float64), ext)
+
+
+def _sign_align(x, ref, axis):
+    s = np.sign(np.sum(x * ref, axis=axis, keepdims=True))
+    s[s == 0] = 1
+    return x * s
+
+
+def nlsa_errors(out, ref):
+    """Differences of an NLSA.op result from a reference result, each eigenvector-derived array
+    aligned in sign first (IMGT, sdiag and mu do not depend on eigenvector signs; tau is compared
+    with 1 - tau_ref when the third psirec column has the opposite sign)."""
+    from scipy.linalg import subspace_angles
+    IMGT, Topo, psirec, psiC1, sdiag, VX, mu, tau = out
+    r_IMGT, r_Topo, r_psirec, r_psiC1, r_sdiag, r_VX, r_mu, r_tau = ref
+    flip = np.sum(psirec[:, 2] * r_psirec[:, 2]) < 0
+    return dict(
+        IMGT=float(np.abs(IMGT - r_IMGT).max()),
+        sdiag=float((np.abs(sdiag - r_sdiag) / r_sdiag).max()),
+        Topo=float(np.abs(_sign_align(Topo, r_Topo, 0) - r_Topo).max() / np.abs(r_Topo).max()),
+        VX=float(np.abs(_sign_align(VX, r_VX, 1) - r_VX).max() / np.abs(r_VX).max()),
+        psiC1=float(np.abs(_sign_align(psiC1, r_psiC1, 0) - r_psiC1)[:, :3].max()),
+        psirec=float(np.abs(_sign_align(psirec, r_psirec, 0) - r_psirec)[:, :3].max()),
+        psirec8=float(np.max(subspace_angles(psirec[:, :8], r_psirec[:, :8]))),
+        mu=float(np.abs(mu - r_mu).max()),
+        tau=float(np.abs(tau - ((1 - r_tau) if flip else r_tau)).max()),
+    )
+
+
+def nlsa_golden_ref(g, tag):
+    return tuple(g['%s_%s' % (tag, k)].astype(np.float64) for k in
+                 ('IMGT', 'Topo_mean', 'psirec', 'psiC1', 'sdiag', 'VX', 'mu', 'tau'))

@@ -118,11 +118,12 @@ FULL_KEEP = ['D', 'ind', 'q', 'df', 'CTF', 'imgAll', 'PD', 'PDs', 'Psis', 'imgAv
 SLICE_KEYS = ['CTF', 'imgAll', 'imgAllFlip']
 
 
-def make_case(name):
+def run_reference_distance(name, synth_over, mic_over, opt_over):
+    """The reference's distance stage on a seeded synthetic PD: (pickle dict, fixture inputs)."""
     sys.path.insert(0, REPO)
     from manifoldem_python_gb300.synthetic import CONFIGS, make_dataset
     ref_p, ref_op = load_reference()
-    synth_over, mic_over, opt_over, slice_idx = CASES[name]
+    mic_over = dict(mic_over)
     cfg = dataclasses.replace(CONFIGS['config1'], name=name, **synth_over)
     ds = make_dataset(cfg, device='cpu')
     stack16 = ds.stack.numpy().astype(np.float16)
@@ -178,6 +179,12 @@ def make_case(name):
                ref_version=np.array(res['version']), ref_msk2=np.array(res['msk2']),
                mask_volume=(mvol.astype(np.uint8) if mvol is not None else np.zeros(0, np.uint8)),
                ref_CTF_shape=np.array(np.shape(res['CTF'])))
+    return res, rec
+
+
+def make_case(name):
+    synth_over, mic_over, opt_over, slice_idx = CASES[name]
+    res, rec = run_reference_distance(name, synth_over, mic_over, opt_over)
     for k in FULL_KEEP:
         if slice_idx is not None and k in SLICE_KEYS:
             rec['ref_%s_slices' % k] = np.asarray(res[k])[slice_idx]
@@ -185,7 +192,7 @@ def make_case(name):
             rec['ref_' + k] = np.asarray(res[k])
     if slice_idx is not None:
         rec['slice_idx'] = np.array(slice_idx)
-    if not options['avgOnly'] and ind.shape[0] >= 40:
+    if not rec['avgOnly'] and rec['ind'].shape[0] >= 40:
         lamb, psi, sigma = reference_dm(res['D'])
         rec.update(ref_dm_lambda=lamb, ref_dm_psi8=psi[:, :8], ref_dm_sigma=sigma)
     path = os.path.join(HERE, name + '.npz')
@@ -193,7 +200,61 @@ def make_case(name):
     print('wrote', path, os.path.getsize(path) // 1024, 'KiB')
 
 
+# NLSA cases: the reference's NLSA.op (modules/NLSA.py:23-158) on the outputs of its own
+# distance stage, driven as psiAnalysisParS2.op drives it (:57-96): posPath = all images, the
+# images ordered along diffusion coordinate 0 of D, ConOrder = floor(nS / conOrderRange) with
+# conOrderRange 50, psiTrunc 8, tune 3.  Three runs on the same PD: the Wiener branch ('prD')
+# with msk2 = 1, the Wiener branch with a 2D mask, and the unfiltered 'cuti' branch.  imgAll and
+# CTF are rounded to float32 first so that the fixture stores the exact inputs at half size.
+NLSA_CASES = {
+    'nlsa32': dict(N=32, n_pd=1, n_fixed=160, seed=107),
+}
+NLSA_OUT = ['IMGT', 'Topo_mean', 'psirec', 'psiC1', 'sdiag', 'VX', 'mu', 'tau']
+
+
+def nlsa_disc_mask(N):
+    y, x = np.mgrid[0:N, 0:N]
+    return ((x - 0.5 * N + 1.5) ** 2 + (y - 0.5 * N) ** 2) < (0.38 * N) ** 2
+
+
+def make_nlsa_case(name, seed=5):
+    res, _ = run_reference_distance(name, NLSA_CASES[name], {}, {})
+    import NLSA                                         # noqa: E402
+    D = np.asarray(res['D'], dtype=np.float64)
+    imgAll = np.asarray(res['imgAll'], dtype=np.float32)
+    nS = D.shape[0]
+    N = imgAll.shape[1]
+    # the pickle holds CTF as (nS, N^2); psiAnalysisParS2.py:73-74 reshapes it
+    CTF = np.asarray(res['CTF'], dtype=np.float32).reshape(nS, N, N)
+    _, psi, _ = reference_dm(D, seed=0)
+    posPath = np.arange(nS)
+    PosPsi1 = np.argsort(psi[:, 0])
+    DD = D[posPath][:, posPath][PosPsi1][:, PosPsi1]
+    ConOrder = int(np.floor(float(nS) / 50))
+    par = dict(num=nS, ConOrder=ConOrder, k=nS - ConOrder, tune=3, nS=nS, save=False,
+               psiTrunc=8)
+    disc = nlsa_disc_mask(N)
+    rec = dict(D=D, imgAll=imgAll, CTF=CTF, PosPsi1=PosPsi1, ConOrder=np.int64(ConOrder),
+               msk_disc=disc, seed=np.int64(seed))
+    runs = {'a': (np.array(res['msk2']), dict(outDir='', prD=0)),
+            'b': (disc, dict(outDir='', prD=0)),
+            'c': (np.array(1), dict(cuti=0))}
+    for tag, (msk2, ext) in runs.items():
+        np.random.seed(seed)
+        out = NLSA.op(dict(par), DD.copy(), posPath, PosPsi1, imgAll.astype(np.float64), msk2,
+                      CTF.astype(np.float64), ext)
+        for key, val in zip(NLSA_OUT, out):
+            val = np.asarray(val, dtype=np.float64)
+            rec['%s_%s' % (tag, key)] = val.astype(np.float32) if key == 'IMGT' else val
+    path = os.path.join(HERE, name + '.npz')
+    np.savez_compressed(path, **rec)
+    print('wrote', path, os.path.getsize(path) // 1024, 'KiB')
+
+
 if __name__ == '__main__':
-    names = sys.argv[1:] or list(CASES)
+    names = sys.argv[1:] or list(CASES) + list(NLSA_CASES)
     for n in names:
-        make_case(n)
+        if n in NLSA_CASES:
+            make_nlsa_case(n)
+        else:
+            make_case(n)
