@@ -179,6 +179,136 @@ def dm_report(outs, counts, n_sample, cores):
                        'CPU: FP64 port of DMembeddingII/fergusonE/slaplacianonFly (oracle/)')
 
 
+def _oracle_nlsa(task):
+    """Worker: the FP64 restatement of NLSA.op (the reference's per-image Wiener loop) on one
+    PD; (seconds, result)."""
+    args, seed = task
+    from oracle.nlsa_oracle import nlsa
+    np.random.seed(seed)
+    t0 = time.perf_counter()
+    out = nlsa(*args)
+    return time.perf_counter() - t0, out
+
+
+def nlsa_report(ds, params, dev, cores, n_cpu_max=800):
+    """NLSA stage (NLSA.op, the consumer of imgAll / CTF / D, reference modules/NLSA.py:23-158)
+    on three of the benchmark's own PDs (smallest, median and largest image count): their
+    imgAll, CTF and D from the distance stage, the images ordered along diffusion coordinate 0
+    and ConOrder = floor(n / 50), as psiAnalysisParS2.op drives it.  GPU NLSA.op wall time per
+    PD; the snapshot matrix (mem_nlsa_snapshots: spectra, Wiener denominators, banded
+    correlation, inverse transforms) timed alone with CUDA events on the largest PD; the FP64
+    CPU port timed on the host cores for the PDs with n <= n_cpu_max (one process per PD), and
+    its largest differences from the GPU results."""
+    import multiprocessing as mp
+    import torch
+    from manifoldem_python_gb300 import DMembeddingII, NLSA
+    from manifoldem_python_gb300.pipeline import DistanceStage, PdJob
+    counts = np.array([len(ind) for ind in ds.CG])
+    order = np.argsort(counts, kind='stable')
+    pick = list(dict.fromkeys([int(order[0]), int(order[len(order) // 2]), int(order[-1])]))
+    stage = DistanceStage(params)
+    jobs = [PdJob(ind=ds.CG[p].astype(np.int64), q=ds.q[:, ds.CG[p]], df=ds.df[ds.CG[p]])
+            for p in pick]
+    res = stage.run(jobs, ds.stack, ds.nStot, outputs=('D', 'img_all', 'ctf'))
+    runs = []
+    for r in res:
+        D = np.asarray(r['D'], dtype=np.float64)
+        n = D.shape[0]
+        N = params.N
+        np.random.seed(0)
+        psi = DMembeddingII.op(D, n, 3, 60000)[1]
+        P = np.argsort(psi[:, 0])
+        c = n // 50
+        par = dict(num=n, ConOrder=c, k=n - c, tune=3, nS=n, save=False, psiTrunc=8)
+        runs.append((par, D[P][:, P], np.arange(n), P,
+                     np.asarray(r['img_all'], dtype=np.float64),
+                     np.array(1), np.asarray(r['ctf'], dtype=np.float64).reshape(n, N, N),
+                     dict(outDir='', prD=0)))
+    del res
+    np.random.seed(1)
+    NLSA.op(*runs[0])                                     # warm-up
+    gpu_ms, outs = [], []
+    for a in runs:
+        np.random.seed(1)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        outs.append(NLSA.op(*a))
+        torch.cuda.synchronize(dev)
+        gpu_ms.append(1e3 * (time.perf_counter() - t0))
+    # the snapshot matrix alone on the largest PD, device time
+    big = runs[-1]
+    n, c = big[0]['num'], big[0]['ConOrder']
+    g = NLSA._Gpu(dev)
+    images = g.tensor(big[4], torch.float32, big[3])
+    ctf = g.tensor(big[6], torch.float32, big[3])
+    snap_ms, snap_tflops = nlsa_snapshot_timing(images, ctf, n, c, dev, 5)
+    del images, ctf
+    # CPU port on the smaller PDs
+    cpu = [i for i, a in enumerate(runs) if a[0]['num'] <= n_cpu_max]
+    os.environ.setdefault('OMP_NUM_THREADS', '1')
+    os.environ.setdefault('OPENBLAS_NUM_THREADS', '1')
+    cpu_s, err = [], {}
+    if cpu:
+        with mp.get_context('spawn').Pool(processes=min(cores, len(cpu))) as pool:
+            got = pool.map(_oracle_nlsa, [(runs[i], 1) for i in cpu], chunksize=1)
+        for i, (sec, ref) in zip(cpu, got):
+            cpu_s.append(sec)
+            o = outs[i]
+            flip = np.sum(o[2][:, 2] * ref[2][:, 2]) < 0
+            tau_ref = (1 - ref[7]) if flip else ref[7]
+            for key, v in (('IMGT_max_abs', np.abs(o[0] - ref[0]).max()),
+                           ('sdiag_max_rel', (np.abs(o[4] - ref[4]) / ref[4]).max()),
+                           ('tau_max_abs', np.abs(o[7] - tau_ref).max())):
+                err[key] = max(err.get(key, 0.0), float(v))
+    return dict(pds=len(runs), n=[int(a[0]['num']) for a in runs],
+                con_order=[int(a[0]['ConOrder']) for a in runs],
+                gpu_ms_per_pd=gpu_ms,
+                snapshots_ms_largest=snap_ms,
+                snapshots_correlation_tflops=snap_tflops,
+                cpu_n=[int(runs[i][0]['num']) for i in cpu],
+                cpu_ms_per_pd_one_core=[1e3 * t for t in cpu_s],
+                gpu_vs_cpu_port=err,
+                method='GPU: csrc/nlsa.cu (ConD, Wiener snapshot correlation), GPU diffusion '
+                       'maps, torch GEMMs, host fit; CPU: FP64 port of NLSA.op with the '
+                       "reference's per-image FFT loop (oracle/nlsa_oracle.py)")
+
+
+def nlsa_snapshot_timing(images, ctf, n, c, dev, reps):
+    """Device time (CUDA events on the launching stream) of mem_nlsa_snapshots for one PD:
+    ms per call and the correlation's algorithmic TFLOP/s (4 c (n - c) K 8 flops, K half-plane
+    frequencies, 8 modes)."""
+    import torch
+    from manifoldem_python_gb300 import NLSA
+    g = NLSA._Gpu(dev)
+    N = int(images.shape[-1])
+    mu_psi = np.random.default_rng(0).standard_normal((n - c, 8)) / n
+    NLSA.snapshots(g, images, ctf, mu_psi, np.array(1), c)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(g.stream)
+    for _ in range(reps):
+        NLSA.snapshots(g, images, ctf, mu_psi, np.array(1), c)
+    e1.record(g.stream)
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1) / reps
+    flop = 4.0 * c * (n - c) * N * (N // 2 + 1) * 8
+    return ms, flop / (ms * 1e-3) / 1e12
+
+
+def nlsa_snapshot_case(ds, params, dev, reps):
+    """The snapshot matrix alone for the PD of ds (its distance-stage images and CTFs)."""
+    import torch
+    from manifoldem_python_gb300.pipeline import DistanceStage, PdJob
+    ind = ds.CG[0].astype(np.int64)
+    r = DistanceStage(params).run([PdJob(ind=ind, q=ds.q[:, ind], df=ds.df[ind])], ds.stack,
+                                  ds.nStot, outputs=('img_all', 'ctf'))[0]
+    n, N = len(ind), params.N
+    images = torch.as_tensor(np.asarray(r['img_all'], dtype=np.float32)).to(dev)
+    ctf = torch.as_tensor(np.asarray(r['ctf'], dtype=np.float32).reshape(n, N, N)).to(dev)
+    c = n // 50
+    ms, tflops = nlsa_snapshot_timing(images, ctf, n, c, dev, reps)
+    return dict(n=n, con_order=c, snapshots_ms=ms, snapshots_correlation_tflops=tflops)
+
+
 def run_cpu_tasks(tasks, cores):
     import multiprocessing as mp
     os.environ.setdefault('OMP_NUM_THREADS', '1')
@@ -356,6 +486,9 @@ def run_gpu(args, rank, world):
     dm = None
     if not args.no_dm and 'D' in outs and rank == 0:
         dm = dm_report(outs, counts, args.dm_pds, os.cpu_count() or 1)
+    nlsa = None
+    if not args.no_nlsa and rank == 0:
+        nlsa = nlsa_report(ds, params, dev, os.cpu_count() or 1)
 
     # end to end through the public API with host buffers
     e2e = None
@@ -421,6 +554,7 @@ def run_gpu(args, rank, world):
     return dict(ms=ms, pairs=n_pairs, n_images=n_images, counts=counts,
                 graph=graph_used, l2_flush=flush,
                 phases=phases, clocks=clk.summary(), t_gen=t_gen, e2e=e2e, ds=ds, cfg=cfg, dm=dm,
+                nlsa=nlsa,
                 kernels=kernels_per_execute(outputs, False, cfg.N), outputs=outputs)
 
 
@@ -536,6 +670,14 @@ def main():
     ap.add_argument('--no-dm', action='store_true',
                     help='skip the diffusion-map embedding of a sample of PDs (GPU vs CPU port)')
     ap.add_argument('--dm-pds', type=int, default=8)
+    ap.add_argument('--no-nlsa', action='store_true',
+                    help='skip the NLSA-stage report (GPU NLSA.op against the CPU port)')
+    ap.add_argument('--nlsa-case', default='',
+                    help='"N,n": run only the NLSA report on one synthetic PD of n images of '
+                         'N px (its distance-stage outputs as input) and print it as JSON')
+    ap.add_argument('--nlsa-snapshots-only', action='store_true',
+                    help='with --nlsa-case: time only the snapshot matrix (mem_nlsa_snapshots) '
+                         'of the PD, ConOrder = floor(n / 50), 8 modes, --steps launches')
     ap.add_argument('--no-precision', action='store_true',
                     help='skip the FP64 / diffusion-map precision report of one sample PD')
     ap.add_argument('--cpu-max-n', type=int, default=900)
@@ -546,6 +688,25 @@ def main():
     world = int(os.environ.get('WORLD_SIZE', '1'))
     rank = int(os.environ.get('RANK', '0'))
     metric = 'all-PD CTF-distance pairs/s'
+
+    if args.nlsa_case:
+        import dataclasses
+        import torch
+        from manifoldem_python_gb300.pipeline import StageParams
+        from manifoldem_python_gb300.synthetic import CONFIGS, make_dataset
+        N, n = (int(v) for v in args.nlsa_case.split(','))
+        cfg = dataclasses.replace(CONFIGS['config1'], name='nlsa', N=N, n_pd=1, n_fixed=n,
+                                  seed=5)
+        dev = torch.device('cuda')
+        ds = make_dataset(cfg, device=dev)
+        params = StageParams(N=N, pix_size=cfg.pix, Cs=cfg.cs, EkV=cfg.kv, AmpContrast=cfg.ampc)
+        if args.nlsa_snapshots_only:
+            rep = nlsa_snapshot_case(ds, params, dev, args.steps)
+        else:
+            rep = nlsa_report(ds, params, dev, os.cpu_count() or 1,
+                              n_cpu_max=0 if args.no_cpu_baseline else 800)
+        print(json.dumps(dict(nlsa_case=dict(N=N, n=n), nlsa=rep)))
+        return
 
     if args.impl == 'reference':
         if rank != 0:
@@ -633,6 +794,8 @@ def main():
                            ms_per_step=e['ms'], pinned=e['pinned'], mode=e['mode'])
     if r.get('dm'):
         line['dm_embedding'] = r['dm']
+    if r.get('nlsa'):
+        line['nlsa'] = r['nlsa']
     if not args.no_precision:
         line['precision'] = precision_report(args, r['ds'], r['counts'], cfg, args.precision)
     if not args.no_cpu_baseline:

@@ -35,7 +35,7 @@ constexpr int kLags = 4;           // lags ii per thread
 constexpr int kCorrThreads = 128;
 constexpr int kMuRows = 256;       // mu_psi rows staged in shared memory at a time
 constexpr int kWienerChunk = 64;   // Wiener denominators per thread (sliding window)
-constexpr int64_t kTargetThreads = 152 * 1024;   // correlation threads aimed for (chunks S)
+constexpr int64_t kTargetThreads = 152 * 4096;   // correlation threads aimed for (chunks S)
 
 inline size_t align_up(size_t x) { return (x + 255) / 256 * 256; }
 
@@ -61,7 +61,7 @@ NlsaLayout nlsa_layout(int N, int num, int c, int T, bool wiener) {
     L.groups = (T + kModes - 1) / kModes;
     const int64_t lag_blocks = (c + kLags - 1) / kLags;
     int64_t S = (kTargetThreads + L.K * lag_blocks - 1) / (L.K * lag_blocks);
-    S = std::max<int64_t>(1, std::min<int64_t>({S, 32, (int64_t)m}));
+    S = std::max<int64_t>(1, std::min<int64_t>({S, 64, (int64_t)m}));
     L.chunk = (int)((m + S - 1) / S);
     L.S = (m + L.chunk - 1) / L.chunk;
     L.smem_fft = wiener && (N == 32 || N == 64 || N == 128);
@@ -113,7 +113,8 @@ __global__ void twiddle_kernel(int N, float2* __restrict__ tw) {
 
 // rw[i][k] = 1 / wd_i(k), wd_i = sum_{t = i+1 .. i+c} C_t(k)^2 + 1/5 (get_wiener.py:14-19), C_t(k)
 // = ctf[t][ky][kx] for half-plane frequency k = ky Nh + kx.  Each thread starts its chunk of i
-// with the direct sum (t = i+c first, as the reference adds) and slides it in float64.
+// with the direct sum (t = i+c first, as the reference adds) and slides it in float64; the
+// reciprocal is taken in float32 (the correlation's precision).
 __global__ void wiener_kernel(const float* __restrict__ ctf, int N, int Nh, int64_t K, int c,
                               int m, float* __restrict__ rw) {
     const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -130,7 +131,7 @@ __global__ void wiener_kernel(const float* __restrict__ ctf, int N, int Nh, int6
         w += v * v;
     }
     for (int i = i0; i < i1; ++i) {
-        rw[(int64_t)i * K + k] = (float)(1.0 / (w + 0.2));
+        rw[(int64_t)i * K + k] = __frcp_rn((float)(w + 0.2));
         if (i + 1 < i1) {
             const double a = C[(int64_t)(i + 1 + c) * NN], b = C[(int64_t)(i + 1) * NN];
             w += a * a - b * b;
