@@ -511,7 +511,8 @@ def run_gpu(args, rank, world):
             del stack
             torch.cuda.empty_cache()
             st = StreamedStage(params, counts, [g.psi_p for g in geoms], n_groups=args.e2e_groups,
-                               outputs=res_names, device=dev)
+                               outputs=res_names, device=dev, ramp=args.e2e_ramp,
+                               ramp_steps=args.e2e_ramp_steps)
             st.set_metadata(sidx_h, flip_h, psi_h, df_h)
             h2d = stack_h.numel() * 4 + st.metadata_bytes()
             d2h = st.result_bytes()
@@ -519,7 +520,8 @@ def run_gpu(args, rank, world):
             def e2e_step():
                 st.run(stack_h)
             mode = 'streamed: stack in pinned host memory read by the load kernels over the host ' \
-                   'link, %d PD groups on load / compute / copy streams' % len(st.groups)
+                   'link, %d PD groups (image counts %s) on load / compute / copy streams' % (
+                       len(st.groups), [int(sum(counts[i] for i in g)) for g in st.groups])
         else:
             meta_h = [torch.from_numpy(x).pin_memory() if pin else torch.from_numpy(x)
                       for x in (sidx_h, flip_h, psi_h, df_h)]
@@ -666,7 +668,10 @@ def main():
                     help='streamed: stack left in pinned host memory, PD groups pipelined over '
                          'load / compute / copy streams; copy: one host-to-device copy of the '
                          'stack, then one execute')
-    ap.add_argument('--e2e-groups', type=int, default=8)
+    ap.add_argument('--e2e-groups', type=int, default=10)
+    ap.add_argument('--e2e-ramp', type=float, default=1.5,
+                    help='growth factor of the first PD groups of the streamed e2e pass')
+    ap.add_argument('--e2e-ramp-steps', type=int, default=4)
     ap.add_argument('--no-dm', action='store_true',
                     help='skip the diffusion-map embedding of a sample of PDs (GPU vs CPU port)')
     ap.add_argument('--dm-pds', type=int, default=8)

@@ -315,14 +315,26 @@ def relion_shifts(stack_index: np.ndarray, sh) -> np.ndarray:
     return out
 
 
-def balanced_groups(counts: Sequence[int], n_groups: int) -> List[range]:
-    """Consecutive PD ranges with about equal image counts (at most n_groups, none empty)."""
+def group_weights(n_groups: int, ramp: float = 1.0, ramp_steps: int = 0) -> np.ndarray:
+    """Relative image counts of the groups: ramp^min(g, ramp_steps) for group g (all equal for
+    ramp 1 or ramp_steps 0)."""
+    g = np.arange(max(1, int(n_groups)))
+    return float(ramp) ** np.minimum(g, max(0, int(ramp_steps)))
+
+
+def balanced_groups(counts: Sequence[int], n_groups: int, ramp: float = 1.0,
+                    ramp_steps: int = 0) -> List[range]:
+    """Consecutive PD ranges (at most n_groups, none empty) whose image counts follow
+    group_weights: equal by default; with ramp > 1 the first ramp_steps groups grow
+    geometrically, so that a pipeline that loads group g + 1 while it computes group g starts
+    computing after loading a small first group."""
     counts = np.asarray(counts, dtype=np.int64)
     n_groups = max(1, min(int(n_groups), len(counts)))
+    w = np.cumsum(group_weights(n_groups, ramp, ramp_steps))
     cum = np.cumsum(counts)
     cuts = [0]
     for g in range(1, n_groups):
-        c = int(np.searchsorted(cum, cum[-1] * g / n_groups, side='left')) + 1
+        c = int(np.searchsorted(cum, cum[-1] * w[g - 1] / w[-1], side='left')) + 1
         cuts.append(min(max(c, cuts[-1] + 1), len(counts) - (n_groups - g)))
     cuts.append(len(counts))
     return [range(a, b) for a, b in zip(cuts[:-1], cuts[1:])]
@@ -331,8 +343,11 @@ def balanced_groups(counts: Sequence[int], n_groups: int) -> List[range]:
 class StreamedStage:
     """The stage for many PDs with the image stack left in pinned host memory.
 
-    The PDs are split into ``n_groups`` consecutive groups of about equal image count, one plan
-    each.  Every ``run`` issues, per group, the per-image metadata copy and the stack-reading
+    The PDs are split into ``n_groups`` consecutive groups, one plan each, of about equal image
+    count after a geometric ramp over the first ``ramp_steps`` groups (``balanced_groups``): the
+    host link delivers images about 1.5x faster than the stage computes them, so each group may
+    be up to that much larger than the one before without the compute stream waiting, and a
+    small first group shortens the wait before the first computation.  Every ``run`` issues, per group, the per-image metadata copy and the stack-reading
     kernel on a high-priority load stream (a small grid reading the images over the host link,
     ``mem_plan_execute_split``), the rest of the stage on a compute stream, and the copy of the
     results into pinned host buffers on a copy stream.  Group g+1's images arrive while group g
@@ -340,12 +355,12 @@ class StreamedStage:
     """
 
     def __init__(self, params: StageParams, counts: Sequence[int], psi_p: Sequence[float],
-                 n_groups: int = 4, outputs=('D', 'img_avg', 'img_avg_flip', 'img_all_intensity'),
-                 device=None):
+                 n_groups: int = 10, outputs=('D', 'img_avg', 'img_avg_flip', 'img_all_intensity'),
+                 device=None, ramp: float = 1.5, ramp_steps: int = 4):
         import torch
         self.device = torch.device(device or 'cuda')
         self.counts = [int(c) for c in counts]
-        self.groups = balanced_groups(self.counts, n_groups)
+        self.groups = balanced_groups(self.counts, n_groups, ramp, ramp_steps)
         psi_p = np.asarray(psi_p, dtype=np.float64)
         self.plans = [Plan(params, [self.counts[i] for i in g], psi_p[list(g)], self.device)
                       for g in self.groups]

@@ -84,6 +84,13 @@ def test_balanced_groups_cover_pds_in_order():
         if n_pd >= 100:
             sizes = [int(counts[list(g)].sum()) for g in groups]
             assert max(sizes) - min(sizes) <= 2 * counts.max()
+    # ramped: the first groups grow by the ramp factor, the rest are equal
+    counts = rng.integers(100, 900, 800)
+    groups = balanced_groups(counts, 8, ramp=1.5, ramp_steps=3)
+    assert [i for g in groups for i in g] == list(range(800))
+    sizes = np.array([int(counts[list(g)].sum()) for g in groups], dtype=float)
+    w = np.array([1, 1.5, 2.25, 3.375, 3.375, 3.375, 3.375, 3.375])
+    assert np.abs(sizes / sizes.sum() - w / w.sum()).max() < 2 * counts.max() / sizes.sum()
 
 
 def test_async_writer_writes_pickles_then_markers(tmp_path):
