@@ -137,6 +137,104 @@ std::vector<int32_t> radius_descending_columns(int N, int64_t Kc, int64_t Kc_pad
     for (int64_t k = 0; k < Kc_pad; ++k) col[k] = (int32_t)(pos[k / kKPad] * kKPad + k % kKPad);
     return col;
 }
+
+// Feature layout.  Ring features: the C^2 |F|^2 part of D, sum_k w C_j(k)^2 |F_i(k)|^2, depends on
+// the CTF only through |k|^2 (C is radial), so it is a sum over rings of equal |k|^2 of
+// C_j(ring)^2 times the ring sums of w |F_i|^2: U', V' get one column per ring instead of one per
+// frequency (1621 rings for 8320 half-plane frequencies at 128 px).  Rings are ordered by
+// decreasing |k|^2, members within a ring by k.  The contraction's K chunks interleave the
+// (U', V') and (r', s') chunk pairs in proportion, so that the low frequencies of both come last.
+void feature_layout(mem_plan* P) {
+    const int N = P->N, Nh = P->Nh;
+    const int64_t Kc = P->Kc;
+    P->Kc_pad = (Kc + kKPad - 1) / kKPad * kKPad;
+    P->colmap = radius_descending_columns(N, Kc, P->Kc_pad);
+    P->ring_features = P->ring_features && Kc <= kRingMaxKc;
+    std::vector<int32_t> ring_start, ring_m, pos_of, ring_of;
+    if (P->ring_features) {
+        std::vector<int64_t> mk(Kc);
+        std::vector<int32_t> order(Kc);
+        for (int64_t k = 0; k < Kc; ++k) {
+            const int ka = (int)(k / Nh), kb = (int)(k % Nh);
+            const int fa = std::min(ka, N - ka);
+            mk[k] = (int64_t)fa * fa + (int64_t)kb * kb;
+            order[k] = (int32_t)k;
+        }
+        std::stable_sort(order.begin(), order.end(),
+                         [&](int32_t a, int32_t b) { return mk[a] > mk[b]; });
+        pos_of.resize(Kc);
+        ring_of.resize(Kc);
+        for (int64_t i = 0; i < Kc; ++i) {
+            if (i == 0 || mk[order[i]] != mk[order[i - 1]]) {
+                ring_start.push_back((int32_t)i);
+                ring_m.push_back((int32_t)mk[order[i]]);
+            }
+            pos_of[order[i]] = (int32_t)i;
+            ring_of[order[i]] = (int32_t)ring_m.size() - 1;
+        }
+        ring_start.push_back((int32_t)Kc);
+        P->Kr = (int64_t)ring_m.size();
+        P->Kr_pad = (P->Kr + kKPad - 1) / kKPad * kKPad;
+    } else {
+        ring_start.push_back(0);
+        P->Kr = Kc;
+        P->Kr_pad = P->Kc_pad;
+    }
+    P->Kf = 2 * P->Kr_pad + 2 * P->Kc_pad;
+    const int64_t Kr_pad = P->Kr_pad, Kc_pad = P->Kc_pad;
+    std::vector<int4> ch;
+    const int64_t nu = Kr_pad / kKPad, nr = Kc_pad / kKPad;
+    // w = 1: the split-BF16 contraction adds the lo.lo product for the chunk.  Ring sums are
+    // fewer and larger terms than per-frequency products, so their split error weighs more; the
+    // largest are the low-frequency rings of the last 4 (U', V') chunk pairs
+    // (MEM_RING_LOLO_PAIRS overrides the count, for tuning)
+    int64_t lolo_pairs = 4;
+    if (const char* e = std::getenv("MEM_RING_LOLO_PAIRS")) lolo_pairs = std::atoll(e);
+    auto push_uv = [&](int64_t q) {
+        const int lolo = (P->ring_features && q >= nu - lolo_pairs) ? 1 : 0;
+        ch.push_back(make_int4((int)(q * kKPad), (int)(Kr_pad + q * kKPad), 0, lolo));
+        ch.push_back(make_int4((int)(Kr_pad + q * kKPad), (int)(q * kKPad), 0, lolo));
+    };
+    auto push_rs = [&](int64_t q) {
+        const int a = (int)(2 * Kr_pad + q * kKPad), b = (int)(2 * Kr_pad + Kc_pad + q * kKPad);
+        ch.push_back(make_int4(a, a, 1, 0));
+        ch.push_back(make_int4(b, b, 1, 0));
+    };
+    if (!P->ring_features) {
+        for (int64_t q = 0; q < nr; ++q) {      // u', v', r', s' chunk q in turn
+            push_uv(q);
+            push_rs(q);
+        }
+    } else {
+        int64_t i = 0, j = 0;
+        while (i < nu || j < nr) {
+            if (j >= nr || (i < nu && (2 * i + 1) * nr <= (2 * j + 1) * nu))
+                push_uv(i++);
+            else
+                push_rs(j++);
+        }
+    }
+    P->n_chunks = (int)ch.size();
+    // one int32 table: colmap | ring_start | ring_m | pos_of | ring_of | chunks (16-byte aligned)
+    std::vector<int32_t>& t = P->ftab;
+    t.assign(P->colmap.begin(), P->colmap.end());
+    P->ft_ring_start = t.size();
+    t.insert(t.end(), ring_start.begin(), ring_start.end());
+    P->ft_ring_m = t.size();
+    t.insert(t.end(), ring_m.begin(), ring_m.end());
+    P->ft_pos_of = t.size();
+    t.insert(t.end(), pos_of.begin(), pos_of.end());
+    P->ft_ring_of = t.size();
+    t.insert(t.end(), ring_of.begin(), ring_of.end());
+    while (t.size() % 4) t.push_back(0);
+    P->ft_chunks = t.size();
+    for (const int4& c : ch) {
+        t.push_back(c.x);
+        t.push_back(c.y);
+        t.push_back(c.z);
+        t.push_back(c.w);
+    }
+}
 namespace {
 
 CtfConst make_ctf(const mem_params& p, int N) {
@@ -224,7 +322,9 @@ int mem_plan_create(const mem_params* params, int32_t n_pd, const int32_t* pd_co
     P->N = p.N;
     P->Nh = p.N / 2 + 1;
     P->Kc = (int64_t)P->N * P->Nh;
-    P->Kc_pad = (P->Kc + kKPad - 1) / kKPad * kKPad;
+    // ring features for the U', V' blocks (MEM_RING_FEATURES=0 selects per-frequency blocks)
+    if (const char* e = std::getenv("MEM_RING_FEATURES")) P->ring_features = std::atoi(e) != 0;
+    feature_layout(P);
     P->count.assign(pd_count, pd_count + n_pd);
     P->pd.resize(n_pd);
     int64_t img = 0, row = 0, d = 0, pairs = 0;
@@ -262,7 +362,6 @@ int mem_plan_create(const mem_params* params, int32_t n_pd, const int32_t* pd_co
         return MEM_ERR_UNSUPPORTED;
     }
     P->ctf = make_ctf(p, P->N);
-    P->colmap = radius_descending_columns(P->N, P->Kc, P->Kc_pad);
     // tensor-core accumulation knobs (tuning; the defaults are the validated setting)
     if (const char* e = std::getenv("MEM_TC_GROUP_CHUNKS")) P->tc_group_chunks = std::atoi(e);
     if (const char* e = std::getenv("MEM_TC_KAHAN")) P->tc_kahan = std::atoi(e) != 0;
@@ -321,13 +420,13 @@ int mem_plan_create(const mem_params* params, int32_t n_pd, const int32_t* pd_co
     L.qfix = take(sizeof(uint64_t) * P->n_images);
     L.gtab = take(sizeof(float) * P->N * P->Nh);
     L.pd_max = take(sizeof(uint32_t) * n_pd);
-    L.colmap = take(sizeof(int32_t) * P->Kc_pad);
+    L.colmap = take(sizeof(int32_t) * P->ftab.size());
     L.twid = take(sizeof(float) * 2 * (P->N / 2 + 1));
     L.ident = take(sizeof(int64_t) * P->n_images);      // 0..n-1: stack index of shifted copies
     L.xbuf = take(sizeof(float) * NN * P->n_images);
     L.spec = take(sizeof(float) * 2 * P->Kc * P->n_images);
-    L.feat_a = take(feat_elem * 4 * P->Kc_pad * P->n_rows);
-    L.feat_b = (p.precision == MEM_PREC_FP32) ? L.feat_a : take(feat_elem * 4 * P->Kc_pad * P->n_rows);
+    L.feat_a = take(feat_elem * P->Kf * P->n_rows);
+    L.feat_b = (p.precision == MEM_PREC_FP32) ? L.feat_a : take(feat_elem * P->Kf * P->n_rows);
     L.pair_norm = take(sizeof(double) * P->n_images);
     L.partial = take(sizeof(float) * 6 * P->Kc * P->items.size());
     L.means = take(sizeof(float) * means_stride(*P) * n_pd);
@@ -379,8 +478,8 @@ int mem_plan_upload(mem_plan* plan, void* workspace, size_t workspace_bytes, voi
                                  sizeof(int32_t) * P.n_images, cudaMemcpyHostToDevice, s));
     MEM_CUDA_TRY(cudaMemcpyAsync(at<char>(workspace, L.tiles), P.tiles.data(),
                                  sizeof(Tile) * P.tiles.size(), cudaMemcpyHostToDevice, s));
-    MEM_CUDA_TRY(cudaMemcpyAsync(at<char>(workspace, L.colmap), P.colmap.data(),
-                                 sizeof(int32_t) * P.Kc_pad, cudaMemcpyHostToDevice, s));
+    MEM_CUDA_TRY(cudaMemcpyAsync(at<char>(workspace, L.colmap), P.ftab.data(),
+                                 sizeof(int32_t) * P.ftab.size(), cudaMemcpyHostToDevice, s));
     {
         std::vector<int64_t> ident(P.n_images);
         for (int64_t i = 0; i < P.n_images; ++i) ident[i] = i;
@@ -398,7 +497,7 @@ int mem_plan_upload(mem_plan* plan, void* workspace, size_t workspace_bytes, voi
                                  cudaMemcpyHostToDevice, s));
     // padding rows of the feature matrices stay zero for the whole life of the workspace
     const size_t feat_elem = (P.params.precision == MEM_PREC_FP32) ? 4 : 2;
-    const size_t row_bytes = feat_elem * 4 * P.Kc_pad;
+    const size_t row_bytes = feat_elem * P.Kf;
     for (int i = 0; i < P.n_pd; ++i) {
         const int n = P.pd[i].n;
         const int64_t padded = (int64_t)((n + kRowBlock - 1) / kRowBlock) * kRowBlock;
@@ -562,21 +661,22 @@ int execute_impl(mem_plan* plan, const mem_inputs* in, const mem_outputs* out, v
     uint32_t* pd_max = at<uint32_t>(ws, L.pd_max);
     const SumItem* items = at<SumItem>(ws, L.sum_items);
     const int32_t* item_off = at<int32_t>(ws, L.item_off);
+    const FeatTables ft = feat_tables(P, at<char>(ws, L.colmap));
     if (in->pd_mask) {
         // the Wiener average from the unmasked spectra, then everything else (centring vectors
         // included, so that they centre the features D is computed from) from the masked ones
         MEM_STEP(kern::pd_sums(P, spec, qf, items, partial, 1, s));
-        MEM_STEP(kern::pd_finalize(P, partial, items, item_off, pds, means, avg_spec, pd_max, 1,
-                                   s));
+        MEM_STEP(kern::pd_finalize(P, partial, items, item_off, pds, ft.ring_of, means,
+                                   avg_spec, pd_max, 1, s));
         MEM_STEP(kern::apply_pd_mask(P, img_all, xbuf, in->pd_mask, img_pd, s));
         MEM_STEP(spectrum(xbuf));
         MEM_STEP(kern::pd_sums(P, spec, qf, items, partial, 3, s));
-        MEM_STEP(kern::pd_finalize(P, partial, items, item_off, pds, means, avg_spec, pd_max, 2,
-                                   s));
+        MEM_STEP(kern::pd_finalize(P, partial, items, item_off, pds, ft.ring_of, means,
+                                   avg_spec, pd_max, 2, s));
     } else {
         MEM_STEP(kern::pd_sums(P, spec, qf, items, partial, 3, s));
-        MEM_STEP(kern::pd_finalize(P, partial, items, item_off, pds, means, avg_spec, pd_max, 3,
-                                   s));
+        MEM_STEP(kern::pd_finalize(P, partial, items, item_off, pds, ft.ring_of, means,
+                                   avg_spec, pd_max, 3, s));
     }
     MEM_STEP(mark(5));
     // features of D, a_i, sign(C) F, CTF output
@@ -584,7 +684,7 @@ int execute_impl(mem_plan* plan, const mem_inputs* in, const mem_outputs* out, v
     void* feat_b = at<char>(ws, L.feat_b);
     double* pair_norm = out->pair_norm ? out->pair_norm : at<double>(ws, L.pair_norm);
     const uint32_t* scale_bits = pd_max;
-    MEM_STEP(kern::features(P, spec, qf, pds, img_pd, img_row, at<int32_t>(ws, L.colmap), means,
+    MEM_STEP(kern::features(P, spec, qf, pds, img_pd, img_row, ft, means,
                             scale_bits, feat_a, feat_b, pair_norm, out->ctf, out->spectrum,
                             !P.smem_fft && (out->img_all_flip || out->img_all_intensity), s));
     MEM_STEP(mark(6));
@@ -613,10 +713,10 @@ int execute_impl(mem_plan* plan, const mem_inputs* in, const mem_outputs* out, v
         const Tile* tiles = at<Tile>(ws, L.tiles);
         if (P.params.precision == MEM_PREC_FP32)
             MEM_STEP(kern::gemm_fp32(P, (const float*)feat_a, pair_norm, scale_bits, tiles, pds,
-                                     out->D, s));
+                                     ft.chunks, out->D, s));
         else
             MEM_STEP(kern::gemm_split_bf16(P, feat_a, feat_b, pair_norm, scale_bits, tiles, pds,
-                                           out->D, status, s));
+                                           ft.chunks, out->D, status, s));
     }
     MEM_STEP(mark(9));
 #undef MEM_STEP

@@ -13,26 +13,24 @@ constexpr int TM = 128, TN = 128, BK = 16, NT = 256, APAD = 4;
 __global__ void __launch_bounds__(NT) gemm_fp32_kernel(
         const float* __restrict__ X, const double* __restrict__ pair_norm,
         const uint32_t* __restrict__ scale_bits, const Tile* __restrict__ tiles,
-        const PdDev* __restrict__ pds, double* __restrict__ D, int64_t Kc_pad) {
+        const PdDev* __restrict__ pds, const int4* __restrict__ chunks, double* __restrict__ D,
+        int64_t Kf) {
     __shared__ __align__(16) float As[2][BK][TM + APAD];
     __shared__ __align__(16) float Bs[2][BK][TN + APAD];
     const Tile t = tiles[blockIdx.x];
     const PdDev pd = pds[t.pd];
-    const int64_t K4 = 4 * Kc_pad;
+    const int64_t K4 = Kf;
     const int tid = threadIdx.x;
     const int lrow = tid >> 2, lk = (tid & 3) * 4;
     const float* Abase = X + (pd.row_off + (int64_t)t.I * TM) * K4;
     const float* Bbase = X + (pd.row_off + (int64_t)t.J * TN) * K4;
     const int64_t nstage = K4 / BK;
 
-    // stages interleave the four blocks (u', v', r', s') so that the dominant low-frequency
-    // columns at the end of every block are accumulated last
-    auto acol = [&](int64_t st) -> int64_t { return (st & 3) * Kc_pad + (st >> 2) * BK; };
-    auto bcol = [&](int64_t st) -> int64_t {
-        const int64_t off = (st >> 2) * BK;
-        const int blk = (int)(st & 3);
-        return blk == 0 ? Kc_pad + off : (blk == 1 ? off : blk * Kc_pad + off);
-    };
+    // stage st is the 16-column slice (st & 3) of 64-wide chunk st >> 2 of the plan's chunk
+    // schedule (A column, B column, sign), which interleaves the feature blocks so that the
+    // dominant low-frequency columns are accumulated last
+    auto acol = [&](int64_t st) -> int64_t { return chunks[st >> 2].x + (st & 3) * BK; };
+    auto bcol = [&](int64_t st) -> int64_t { return chunks[st >> 2].y + (st & 3) * BK; };
 
     float4 ra[2], rb[2];
     auto gload = [&](int64_t st) {
@@ -46,7 +44,7 @@ __global__ void __launch_bounds__(NT) gemm_fp32_kernel(
         }
     };
     auto sstore = [&](int buf, int64_t st) {
-        const float sg = (st & 3) < 2 ? 1.0f : -1.0f;
+        const float sg = chunks[st >> 2].z ? -1.0f : 1.0f;
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             const int r = lrow + h * 64;
@@ -123,11 +121,12 @@ __global__ void __launch_bounds__(NT) gemm_fp32_kernel(
 
 namespace kern {
 int gemm_fp32(const mem_plan& P, const float* feat, const double* pair_norm,
-              const uint32_t* scale_bits, const Tile* tiles, const PdDev* pds, double* D,
-              cudaStream_t s) {
+              const uint32_t* scale_bits, const Tile* tiles, const PdDev* pds,
+              const int4* chunks, double* D, cudaStream_t s) {
     if (P.tiles.empty() || !D) return MEM_OK;
+    if ((int64_t)P.n_chunks * 64 != P.Kf) return MEM_ERR_INVALID;
     gemm_fp32_kernel<<<(unsigned)P.tiles.size(), NT, 0, s>>>(feat, pair_norm, scale_bits, tiles, pds,
-                                                             D, P.Kc_pad);
+                                                             chunks, D, P.Kf);
     MEM_LAUNCH_CHECK();
     return MEM_OK;
 }

@@ -3,11 +3,13 @@
 //   D_ij = a_i + a_j + E_ij,  E_ij = u'_i.v'_j + v'_i.u'_j - r'_i.r'_j - s'_i.s'_j
 //
 // Each feature x is stored as x_hi = bf16(x), x_lo = bf16(x - x_hi); E is accumulated as
-// A_hi.B_hi + A_hi.B_lo + A_lo.B_hi (the lo.lo term, ~2^-16 relative, is dropped) on the 5th-gen
+// A_hi.B_hi + A_hi.B_lo + A_lo.B_hi (the lo.lo term, ~2^-16 relative, is dropped except in the
+// chunks the schedule marks, the low-frequency ring-sum chunks of U', V') on the 5th-gen
 // tensor cores: tcgen05.mma kind::f16 (BF16 in, FP32 accumulate in TMEM), operands staged in
 // shared memory by TMA (128-byte swizzle).  B reads the same feature matrix as A with its first
-// two column blocks swapped (TMA coordinates); the r', s' blocks use the instruction
-// descriptor's negate-B bit, so one accumulator holds E.
+// two column blocks swapped: each 64-wide K chunk takes its A and B columns from the plan's
+// chunk schedule (TMA coordinates); the r', s' chunks use the instruction descriptor's
+// negate-B bit, so one accumulator holds E.
 //
 // One CTA per upper-triangle 128 x 128 tile (pd, I, J); 10 warps:
 //   warps 0-7  epilogue: warp w reads TMEM lanes 32*(w%4).. and columns 64*(w/4)..;
@@ -19,6 +21,7 @@
 // Every mbarrier wait is bounded: on expiry the CTA sets the status word's timeout bit, stops
 // issuing, waits (bounded) for its own TMA copies and MMAs, frees its TMEM and returns.
 #include <cuda.h>
+#include <type_traits>
 #include <cudaTypedefs.h>
 
 #include "mem_internal.cuh"
@@ -172,7 +175,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gemm_tc_kernel(
         const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CUtensorMap map_lo,
         const double* __restrict__ pair_norm, const uint32_t* __restrict__ scale_bits,
         const Tile* __restrict__ tiles, const PdDev* __restrict__ pds, double* __restrict__ D,
-        uint32_t* __restrict__ status, int64_t Kc_pad, int group_chunks) {
+        uint32_t* __restrict__ status, const int4* __restrict__ chunks, int nchunks,
+        int group_chunks) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     TcShared* sh = (TcShared*)(smem + TC_STAGES * TC_STAGE_BYTES);
@@ -180,7 +184,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gemm_tc_kernel(
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const Tile t = tiles[blockIdx.x];
     const PdDev pd = pds[t.pd];
-    const int nchunks = (int)(4 * Kc_pad / TC_BK);
     const int gsize = (group_chunks > 0 && group_chunks < nchunks) ? group_chunks : nchunks;
     const int ngroups = (nchunks + gsize - 1) / gsize;
 
@@ -222,12 +225,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gemm_tc_kernel(
                 const uint32_t ph = (uint32_t)(c / TC_STAGES) & 1u;
                 if (c >= TC_STAGES && !mbar_wait(&sh->empty[st], ph ^ 1u, abort_flag, status))
                     break;
-                // chunks interleave the four blocks (u', v', r', s') so that the dominant
-                // low-frequency columns at the end of every block are accumulated last
-                const int blk = c & 3;
-                const int64_t off = (int64_t)(c >> 2) * TC_BK;
-                const int64_t ka = blk * Kc_pad + off;
-                const int64_t kb = blk == 0 ? Kc_pad + off : (blk == 1 ? off : ka);
+                // the chunk schedule interleaves the feature blocks so that the dominant
+                // low-frequency columns of every block are accumulated last
+                const int4 ch = chunks[c];
+                const int ka = ch.x, kb = ch.y;
                 uint8_t* sb = smem + st * TC_STAGE_BYTES;
                 mbar_expect_tx(&sh->full[st], TC_STAGE_BYTES);
                 tma_load_2d(sb + 0 * TC_OPB, &map_hi, &sh->full[st], (int)ka, rowA);
@@ -245,7 +246,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gemm_tc_kernel(
         // ---------------------------------------------------------------- MMA issuer
         if (lane == 0) {
             bool issued_any = false;
+            int4 ch_next = chunks[0];                   // schedule entry, read one chunk ahead
             for (int c = 0; c < nchunks; ++c) {
+                const int4 ch = ch_next;
+                if (c + 1 < nchunks) ch_next = chunks[c + 1];
                 const int st = c % TC_STAGES;
                 const uint32_t ph = (uint32_t)(c / TC_STAGES) & 1u;
                 const int g = c / gsize;
@@ -258,21 +262,29 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gemm_tc_kernel(
                     break;
                 if (!mbar_wait(&sh->full[st], ph, abort_flag, status)) break;
                 tc_fence_after();
-                const bool neg = (c & 3) >= 2;          // r', s' blocks (see the producer)
+                const bool neg = ch.z != 0;             // r', s' blocks (chunk schedule)
                 const uint32_t idesc = neg ? IDESC_NEG : IDESC;
                 const uint32_t d = tmem + (uint32_t)(b * TC_N);
                 const uint32_t sa = smem_u32(smem + st * TC_STAGE_BYTES);
+                // three products per K step; the lo.lo product too for marked chunks (one
+                // branch per chunk, both bodies fully unrolled)
+                auto mma_chunk = [&](auto four) {
 #pragma unroll
-                for (int k = 0; k < TC_BK / 16; ++k) {
-                    const uint64_t ahi = sdesc_sw128(sa + 0 * TC_OPB + k * 32);
-                    const uint64_t alo = sdesc_sw128(sa + 1 * TC_OPB + k * 32);
-                    const uint64_t bhi = sdesc_sw128(sa + 2 * TC_OPB + k * 32);
-                    const uint64_t blo = sdesc_sw128(sa + 3 * TC_OPB + k * 32);
-                    umma_bf16(d, ahi, bhi, idesc, (first && k == 0) ? 0u : 1u);
-                    umma_bf16(d, ahi, blo, idesc, 1u);
-                    umma_bf16(d, alo, bhi, idesc, 1u);
-                    if (LOLO) umma_bf16(d, alo, blo, idesc, 1u);
-                }
+                    for (int k = 0; k < TC_BK / 16; ++k) {
+                        const uint64_t ahi = sdesc_sw128(sa + 0 * TC_OPB + k * 32);
+                        const uint64_t alo = sdesc_sw128(sa + 1 * TC_OPB + k * 32);
+                        const uint64_t bhi = sdesc_sw128(sa + 2 * TC_OPB + k * 32);
+                        const uint64_t blo = sdesc_sw128(sa + 3 * TC_OPB + k * 32);
+                        umma_bf16(d, ahi, bhi, idesc, (first && k == 0) ? 0u : 1u);
+                        umma_bf16(d, ahi, blo, idesc, 1u);
+                        umma_bf16(d, alo, bhi, idesc, 1u);
+                        if (decltype(four)::value) umma_bf16(d, alo, blo, idesc, 1u);
+                    }
+                };
+                if (LOLO || ch.w != 0)
+                    mma_chunk(std::true_type{});
+                else
+                    mma_chunk(std::false_type{});
                 issued_any = true;
                 umma_commit(&sh->empty[st]);
                 if (last) umma_commit(&sh->acc_full[b]);
@@ -371,11 +383,11 @@ PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
     return fn;
 }
 
-int make_map(CUtensorMap* map, const void* base, int64_t K4, int64_t rows) {
+int make_map(CUtensorMap* map, const void* base, int64_t Kf, int64_t rows) {
     auto enc = get_encode();
     if (!enc) return MEM_ERR_CUDA;
-    cuuint64_t dims[2] = {(cuuint64_t)K4, (cuuint64_t)rows};
-    cuuint64_t strides[1] = {(cuuint64_t)(K4 * 2)};
+    cuuint64_t dims[2] = {(cuuint64_t)Kf, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)(Kf * 2)};
     cuuint32_t box[2] = {(cuuint32_t)TC_BK, (cuuint32_t)TC_M};
     cuuint32_t estr[2] = {1, 1};
     CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims,
@@ -390,14 +402,16 @@ int make_map(CUtensorMap* map, const void* base, int64_t K4, int64_t rows) {
 namespace kern {
 int gemm_split_bf16(const mem_plan& P, const void* feat_hi, const void* feat_lo,
                     const double* pair_norm, const uint32_t* scale_bits, const Tile* tiles,
-                    const PdDev* pds, double* D, uint32_t* status, cudaStream_t s) {
+                    const PdDev* pds, const int4* chunks, double* D, uint32_t* status,
+                    cudaStream_t s) {
     if (P.tiles.empty() || !D) return MEM_OK;
-    const int64_t K4 = 4 * P.Kc_pad;
-    if (K4 % TC_BK != 0 || P.n_rows % TC_M != 0) return MEM_ERR_INVALID;
+    // every chunk starts on a 64-column boundary: TMA x offsets are multiples of 8 bf16
+    if (P.Kf % TC_BK != 0 || P.n_rows % TC_M != 0 || (int64_t)P.n_chunks * TC_BK != P.Kf)
+        return MEM_ERR_INVALID;
     CUtensorMap mhi, mlo;
-    int st = make_map(&mhi, feat_hi, K4, P.n_rows);
+    int st = make_map(&mhi, feat_hi, P.Kf, P.n_rows);
     if (st != MEM_OK) return st;
-    st = make_map(&mlo, feat_lo, K4, P.n_rows);
+    st = make_map(&mlo, feat_lo, P.Kf, P.n_rows);
     if (st != MEM_OK) return st;
 #define MEM_TC_LAUNCH(KAHAN, LOLO)                                                             \
     do {                                                                                       \
@@ -405,7 +419,7 @@ int gemm_split_bf16(const mem_plan& P, const void* feat_hi, const void* feat_lo,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize,         \
                                           (int)TC_SMEM));                                      \
         gemm_tc_kernel<KAHAN, LOLO><<<(unsigned)P.tiles.size(), TC_THREADS, TC_SMEM, s>>>(     \
-            mhi, mlo, pair_norm, scale_bits, tiles, pds, D, status, P.Kc_pad,                  \
+            mhi, mlo, pair_norm, scale_bits, tiles, pds, D, status, chunks, P.n_chunks,        \
             P.tc_group_chunks);                                                                \
     } while (0)
     if (P.tc_kahan) {

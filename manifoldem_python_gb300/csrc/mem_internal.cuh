@@ -60,6 +60,20 @@ __device__ __forceinline__ int ctf_sign(int m, uint64_t qf, const CtfConst& cc) 
     return (sph > 0) - (sph < 0);
 }
 
+// device tables of the feature layout (feature_layout): colmap [Kc_pad] = column of frequency
+// slot k within the r' / s' blocks; ring features: ring R = frequencies of |k|^2 = ring_m[R],
+// stored at positions ring_start[R] .. ring_start[R+1] of the ring order, pos_of[k] = position of
+// frequency k, ring_of[k] = its ring; chunks [n_chunks] = (A column, B column, negate B, add the
+// lo.lo product) of each 64-wide K chunk of the contraction
+struct FeatTables {
+    const int32_t* colmap;
+    const int32_t* ring_start;
+    const int32_t* ring_m;
+    const int32_t* pos_of;
+    const int32_t* ring_of;
+    const int4* chunks;
+};
+
 struct Layout {
     size_t status, pd_table, sum_items, img_pd, img_row, tiles;
     size_t item_off, qfix, gtab, pd_max, colmap, twid, ident;
@@ -75,6 +89,13 @@ struct mem_plan {
     int64_t n_images = 0;
     int N = 0, Nh = 0;              // Nh = N/2 + 1
     int64_t Kc = 0, Kc_pad = 0;     // half-plane frequencies, padded to kKPad
+    // feature row: [U' (Kr_pad) | V' (Kr_pad) | r' (Kc_pad) | s' (Kc_pad)], Kf columns; with ring
+    // features U', V' are indexed by rings of equal |k|^2 (Kr rings), else by frequency (Kr = Kc)
+    bool ring_features = true;
+    int64_t Kr = 0, Kr_pad = 0, Kf = 0;
+    int n_chunks = 0;
+    std::vector<int32_t> ftab;      // host image of the FeatTables (int32 words)
+    size_t ft_ring_start = 0, ft_ring_m = 0, ft_pos_of = 0, ft_ring_of = 0, ft_chunks = 0;
     int64_t n_rows = 0;             // feature-matrix rows (padded per PD)
     int64_t d_elems = 0, n_pairs = 0;
     std::vector<int32_t> count;
@@ -148,10 +169,10 @@ int pd_sums(const mem_plan& P, const float2* spec, const uint64_t* qf, const Sum
             float* partial, int which, cudaStream_t s);
 // mode bit 1: Wiener average spectrum; bit 2: centring vectors, scale, phase-flip average
 int pd_finalize(const mem_plan& P, const float* partial, const SumItem* items,
-                const int32_t* item_off, const PdDev* pds, float* means, float2* avg_spec,
-                uint32_t* pd_max, int mode, cudaStream_t s);
+                const int32_t* item_off, const PdDev* pds, const int32_t* ring_of, float* means,
+                float2* avg_spec, uint32_t* pd_max, int mode, cudaStream_t s);
 int features(const mem_plan& P, float2* spec, const uint64_t* qf, const PdDev* pds,
-             const int32_t* img_pd, const int32_t* img_row, const int32_t* colmap,
+             const int32_t* img_pd, const int32_t* img_row, const FeatTables& ft,
              const float* means, const uint32_t* scale_bits, void* feat_a, void* feat_b,
              double* pair_norm, float* ctf_out, float* spectrum_out, bool write_signed,
              cudaStream_t s);
@@ -162,17 +183,36 @@ int intensity(const mem_plan& P, const float* flip_imgs, const PdDev* pds, doubl
 
 // ---- D contraction (gemm_fp32.cu / gemm_tc.cu) ----------------------------------------
 int gemm_fp32(const mem_plan& P, const float* feat, const double* pair_norm,
-              const uint32_t* scale_bits, const Tile* tiles, const PdDev* pds, double* D,
-              cudaStream_t s);
+              const uint32_t* scale_bits, const Tile* tiles, const PdDev* pds,
+              const int4* chunks, double* D, cudaStream_t s);
 int gemm_split_bf16(const mem_plan& P, const void* feat_hi, const void* feat_lo,
                     const double* pair_norm, const uint32_t* scale_bits, const Tile* tiles,
-                    const PdDev* pds, double* D, uint32_t* status, cudaStream_t s);
+                    const PdDev* pds, const int4* chunks, double* D, uint32_t* status,
+                    cudaStream_t s);
 }  // namespace kern
 
 std::vector<int32_t> radius_descending_columns(int N, int64_t Kc, int64_t Kc_pad);
 
-// per-PD centring vectors: means[pd * means_stride + b * Kc_pad + k], blocks b = u, v, r, s
-inline int64_t means_stride(const mem_plan& P) { return 4 * P.Kc_pad; }
+// largest half-plane size for ring features (the features kernel keeps one float per frequency
+// in shared memory); larger boxes use per-frequency U', V' blocks
+constexpr int64_t kRingMaxKc = 40960;
+
+// sets Kc_pad, colmap, the ring tables, Kr, Kr_pad, Kf and the chunk schedule of a plan whose N,
+// Nh, Kc and ring_features are set
+void feature_layout(mem_plan* P);
+
+// device pointers of the feature tables uploaded at `base` (P.ftab copied there)
+inline FeatTables feat_tables(const mem_plan& P, const void* base) {
+    const int32_t* w = static_cast<const int32_t*>(base);
+    return FeatTables{w, w + P.ft_ring_start, w + P.ft_ring_m, w + P.ft_pos_of, w + P.ft_ring_of,
+                      reinterpret_cast<const int4*>(w + P.ft_chunks)};
+}
+
+// per-PD centring vectors: means[pd * means_stride + b * Kc_pad + k], blocks b = u, v, r, s;
+// with ring features a fifth block [Kr_pad] holds the ring means of C^2 (mt)
+inline int64_t means_stride(const mem_plan& P) {
+    return 4 * P.Kc_pad + (P.ring_features ? P.Kr_pad : 0);
+}
 
 // power-of-two feature scale of a PD from the bit pattern of its largest |mean| (host+device)
 __host__ __device__ inline float feature_scale_from_bits(uint32_t bits) {

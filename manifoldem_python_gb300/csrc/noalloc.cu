@@ -13,6 +13,7 @@
 // cuFFT plan).
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <vector>
 
 #include "mem_internal.cuh"
@@ -54,10 +55,10 @@ NoallocLayout layout_for(const mem_plan& P) {
     L.means = take(sizeof(float) * means_stride(P));
     L.avg_spec = take(sizeof(float) * 4 * P.Kc);
     L.pd_max = take(sizeof(uint32_t));
-    L.colmap = take(sizeof(int32_t) * P.Kc_pad);
+    L.colmap = take(sizeof(int32_t) * P.ftab.size());
     L.spec = take(sizeof(float) * 2 * P.Kc * P.n_images);
-    L.feat_a = take(feat_elem * 4 * P.Kc_pad * P.n_rows);
-    L.feat_b = (feat_elem == 4) ? L.feat_a : take(feat_elem * 4 * P.Kc_pad * P.n_rows);
+    L.feat_a = take(feat_elem * P.Kf * P.n_rows);
+    L.feat_b = (feat_elem == 4) ? L.feat_a : take(feat_elem * P.Kf * P.n_rows);
     L.pair_norm = take(sizeof(double) * P.n_images);
     L.total = off;
     return L;
@@ -70,7 +71,8 @@ void one_pd_tables(mem_plan& P, const mem_params& prm, int n) {
     P.N = prm.N;
     P.Nh = prm.N / 2 + 1;
     P.Kc = (int64_t)P.N * P.Nh;
-    P.Kc_pad = (P.Kc + kKPad - 1) / kKPad * kKPad;
+    if (const char* e = std::getenv("MEM_RING_FEATURES")) P.ring_features = std::atoi(e) != 0;
+    feature_layout(&P);
     P.count.assign(1, n);
     P.pd.assign(1, PdDev{0, 0, 0, n, 0, 1.0, 0.0});
     const int nb = (n + kRowBlock - 1) / kRowBlock;
@@ -96,7 +98,6 @@ void one_pd_tables(mem_plan& P, const mem_params& prm, int n) {
     P.ctf.d_fix = fix(std::atan(prm.AmpContrast) / (2.0 * M_PI));
     P.ctf.q_scale = lam / (2.0 * Npix * Npix);
     P.ctf.amp = (float)std::sqrt(1.0 + prm.AmpContrast * prm.AmpContrast);
-    P.colmap = radius_descending_columns(P.N, P.Kc, P.Kc_pad);
     if (std::isinf(prm.gaussEnv) || prm.gaussEnv <= 0.0) {
         P.ctf.env_c = 0.0f;
     } else {
@@ -156,14 +157,14 @@ extern "C" int mem_pd_distances_noalloc(const mem_params* params, int32_t n, con
                                  cudaMemcpyHostToDevice, s));
     MEM_CUDA_TRY(cudaMemcpyAsync(at<char>(ws, L.tiles), P.tiles.data(),
                                  sizeof(Tile) * P.tiles.size(), cudaMemcpyHostToDevice, s));
-    MEM_CUDA_TRY(cudaMemcpyAsync(at<char>(ws, L.colmap), P.colmap.data(),
-                                 sizeof(int32_t) * P.Kc_pad, cudaMemcpyHostToDevice, s));
+    MEM_CUDA_TRY(cudaMemcpyAsync(at<char>(ws, L.colmap), P.ftab.data(),
+                                 sizeof(int32_t) * P.ftab.size(), cudaMemcpyHostToDevice, s));
     // the feature kernel overwrites its spectrum with sign(C) F: work on a copy in the scratch
     MEM_CUDA_TRY(cudaMemcpyAsync(at<char>(ws, L.spec), spectra, sizeof(float) * 2 * P.Kc * n,
                                  cudaMemcpyDeviceToDevice, s));
     // padding rows of the feature matrices must read as zero; the scratch keeps old contents
     const size_t feat_elem = (P.params.precision == MEM_PREC_FP32) ? 4 : 2;
-    const size_t row_bytes = feat_elem * 4 * P.Kc_pad;
+    const size_t row_bytes = feat_elem * P.Kf;
     const size_t pad_rows = (size_t)(P.n_rows - n);
     if (pad_rows) {
         MEM_CUDA_TRY(cudaMemsetAsync(at<char>(ws, L.feat_a) + n * row_bytes, 0, pad_rows * row_bytes, s));
@@ -188,19 +189,20 @@ extern "C" int mem_pd_distances_noalloc(const mem_params* params, int32_t n, con
     double* pair_norm = at<double>(ws, L.pair_norm);
     NA_STEP(kern::qfix(P, in, qf, s));
     NA_STEP(kern::pd_sums(P, spec, qf, at<SumItem>(ws, L.items), at<float>(ws, L.partial), 3, s));
+    const FeatTables ft = feat_tables(P, at<char>(ws, L.colmap));
     NA_STEP(kern::pd_finalize(P, at<float>(ws, L.partial), at<SumItem>(ws, L.items),
-                              at<int32_t>(ws, L.item_off), pds, means,
+                              at<int32_t>(ws, L.item_off), pds, ft.ring_of, means,
                               at<float2>(ws, L.avg_spec), pd_max, 3, s));
     NA_STEP(kern::features(P, spec, qf, pds, at<int32_t>(ws, L.img_pd), at<int32_t>(ws, L.img_row),
-                           at<int32_t>(ws, L.colmap), means, scale_bits, at<char>(ws, L.feat_a),
+                           ft, means, scale_bits, at<char>(ws, L.feat_a),
                            at<char>(ws, L.feat_b), pair_norm, nullptr, nullptr, false, s));
     if (P.params.precision == MEM_PREC_FP32)
         NA_STEP(kern::gemm_fp32(P, at<float>(ws, L.feat_a), pair_norm, scale_bits,
-                                at<Tile>(ws, L.tiles), pds, D, s));
+                                at<Tile>(ws, L.tiles), pds, ft.chunks, D, s));
     else
         NA_STEP(kern::gemm_split_bf16(P, at<char>(ws, L.feat_a), at<char>(ws, L.feat_b),
-                                      pair_norm, scale_bits, at<Tile>(ws, L.tiles), pds, D,
-                                      at<uint32_t>(ws, L.status), s));
+                                      pair_norm, scale_bits, at<Tile>(ws, L.tiles), pds,
+                                      ft.chunks, D, at<uint32_t>(ws, L.status), s));
 #undef NA_STEP
     return MEM_OK;
 }

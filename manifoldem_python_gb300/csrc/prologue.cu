@@ -6,8 +6,8 @@
 // Data layout in HBM (per call):
 //   xbuf   [n_images][N][N] float   raw image (storage orientation), later scratch
 //   spec   [n_images][N][N/2+1] float2   half-plane spectra (cuFFT R2C layout)
-//   feats  [n_rows][4*Kc_pad]  float (FP32 form) or two bf16 matrices hi/lo (split form):
-//          column blocks u' | v' | r' | s' (see features_kernel)
+//   feats  [n_rows][Kf]  float (FP32 form) or two bf16 matrices hi/lo (split form):
+//          column blocks U' | V' | r' | s' (see features_kernel)
 #include <cuda_bf16.h>
 #include <algorithm>
 #include <cmath>
@@ -810,10 +810,13 @@ __global__ void __launch_bounds__(256) pd_sums_kernel(
 __global__ void __launch_bounds__(256) pd_finalize_kernel(
         const float* __restrict__ partial, const SumItem* __restrict__ items,
         const int32_t* __restrict__ item_off, const PdDev* __restrict__ pds,
-        float* __restrict__ means, float2* __restrict__ avg_spec, uint32_t* __restrict__ pd_max,
+        const int32_t* __restrict__ ring_of, float* __restrict__ means,
+        float2* __restrict__ avg_spec, uint32_t* __restrict__ pd_max,
         int N, int Nh, int64_t Kc, int64_t Kc_pad, int64_t mstride, int mode) {
     // mode bit 1: the Wiener average spectrum (from S0..S2); bit 2: centring vectors, scale and
-    // the phase-flipped average spectrum
+    // the phase-flipped average spectrum.  With ring features (ring_of != null) the centring of
+    // v is sw(k) mt(R) with the ring mean mt(R) = S0 / n of C^2 (the same sum for every member
+    // of the ring: C depends on |k|^2 only), and mt(R) goes to the fifth block.
     const int64_t k = blockIdx.y * 256ll + threadIdx.x;
     const int pd = blockIdx.x;
     if (k >= Kc_pad) return;
@@ -841,7 +844,13 @@ __global__ void __launch_bounds__(256) pd_finalize_kernel(
     const int kb = (int)(k % Nh);
     const double w = (kb == 0 || (N % 2 == 0 && kb == N / 2)) ? 1.0 : 2.0;
     const double sw = sqrt(w), s2w = sqrt(2.0 * w);
-    const float mu_u = (float)(sw * S[5] / n), mu_v = (float)(sw * S[0] / n);
+    const float mu_u = (float)(sw * S[5] / n);
+    float mu_v = (float)(sw * S[0] / n);
+    if (ring_of) {
+        const float mt = (float)(S[0] / n);
+        mu_v = (float)sw * mt;
+        mu[4 * Kc_pad + ring_of[k]] = mt;
+    }
     const float mu_r = (float)(s2w * S[1] / n), mu_s = (float)(s2w * S[2] / n);
     mu[k] = mu_u;
     mu[Kc_pad + k] = mu_v;
@@ -864,20 +873,29 @@ __global__ void __launch_bounds__(256) pd_finalize_kernel(
 //   With write_signed the spectrum is overwritten with sign(C) F / N^2 (input of a cuFFT
 //   phase-flip C2R); the shared-memory inverse FFT applies sign(C) / N^2 itself.
 // ------------------------------------------------------------------------------------------
-// MODE 0: FP32 features; 1: bf16 hi/lo.  Frequency slot k (k >= Kc: zero padding) goes to
-// feature column colmap[k]: 64-wide chunks ordered so the dominant low frequencies are
-// accumulated last (radius_descending_columns).
-template <int MODE>
+// MODE 0: FP32 features; 1: bf16 hi/lo.  Feature row: [U' | V' | r' | s'] of widths Kr_pad,
+// Kr_pad, Kc_pad, Kc_pad.  Frequency slot k (k >= Kc: zero padding) goes to column colmap[k] of
+// the r', s' blocks: 64-wide chunks ordered so the dominant low frequencies are accumulated last
+// (radius_descending_columns).
+//   RINGS = false: U' = u', V' = v' per frequency (columns colmap[k]).
+//   RINGS = true: v'_j(k) = sw(k) (C_j(m)^2 - mt(R)) with the ring mean mt(R) of C^2 (m = |k|^2,
+//     R = k's ring; pd_finalize writes the centring sw(k) mt(R) of v and mt), so
+//     sum_k u'_i v'_j = sum_R U_i(R) V_j(R) with U_i(R) = sum_{k in R} sw(k) u'_i(k) and
+//     V_j(R) = C_j(m_R)^2 - mt(R): one column per ring, rings by decreasing |k|^2.  Phase 1
+//     keeps sw u' of every frequency in shared memory at its position in ring order, phase 2
+//     sums each ring's contiguous range.
+template <int MODE, bool RINGS>
 __global__ void __launch_bounds__(256) features_kernel(
         float2* __restrict__ spec, const uint64_t* __restrict__ qfix,
         const PdDev* __restrict__ pds, const int32_t* __restrict__ img_pd,
-        const int32_t* __restrict__ img_row, const int32_t* __restrict__ colmap,
+        const int32_t* __restrict__ img_row, const FeatTables ft,
         const float* __restrict__ means,
         const uint32_t* __restrict__ scale_bits, void* __restrict__ feat_a, void* __restrict__ feat_b,
         double* __restrict__ pair_norm, float* __restrict__ ctf_out,
         float2* __restrict__ spectrum_out, int N, int Nh, int64_t Kc, int64_t Kc_pad,
-        int64_t mstride, CtfConst cc, int write_signed) {
+        int64_t Kr, int64_t Kr_pad, int64_t mstride, CtfConst cc, int write_signed) {
     __shared__ double red[32];
+    extern __shared__ float tbuf[];          // RINGS: sw u' of every frequency (scaled)
     const int64_t img = blockIdx.x;
     const int pd = img_pd[img];
     const int64_t row = img_row[img];
@@ -885,17 +903,21 @@ __global__ void __launch_bounds__(256) features_kernel(
     const float sc = feature_scale_from_bits(scale_bits[pd]);
     const uint64_t qf = qfix[img];
     const float inv_nn = 1.0f / ((float)N * (float)N);
-    const int64_t K4 = 4 * Kc_pad;
+    const int64_t Kf = 2 * Kr_pad + 2 * Kc_pad;
     float2* sp = spec + img * Kc;
     KSum acc;
+    auto weight = [&](int64_t k, int* m_out) {
+        const int ka = (int)(k / Nh), kb = (int)(k - (int64_t)ka * Nh);
+        const int fa = min(ka, N - ka);
+        *m_out = fa * fa + kb * kb;
+        return (kb == 0 || ((N & 1) == 0 && kb == N / 2));     // half-plane weight 1
+    };
     // features (u', v', r', s') of frequency slot k; zero for the padding k >= Kc
     auto feature = [&](int64_t k, float (&f)[4]) {
         f[0] = f[1] = f[2] = f[3] = 0.f;
         if (k >= Kc) return;
-        const int ka = (int)(k / Nh), kb = (int)(k - (int64_t)ka * Nh);
-        const int fa = min(ka, N - ka);
-        const int m = fa * fa + kb * kb;
-        const bool w1 = (kb == 0 || ((N & 1) == 0 && kb == N / 2));
+        int m;
+        const bool w1 = weight(k, &m);
         const float sw = w1 ? 1.0f : 1.41421356237309505f;
         const float s2w = w1 ? 1.41421356237309505f : 2.0f;
         const float2 F = sp[k];
@@ -914,9 +936,23 @@ __global__ void __launch_bounds__(256) features_kernel(
         f[1] = (v - mu_v) * sc;
         f[2] = (r - mu_r) * sc;
         f[3] = (s - mu_s) * sc;
+        if (RINGS) tbuf[ft.pos_of[k]] = sw * f[0];
         if (write_signed) {
             const float sgf = (float)sg * inv_nn;
             sp[k] = make_float2(sgf * F.x, sgf * F.y);
+        }
+    };
+    auto store2 = [&](int64_t col, float a0, float a1) {     // columns col, col + 1 (col even)
+        if (MODE == 1) {
+            __nv_bfloat162* hi = (__nv_bfloat162*)((__nv_bfloat16*)feat_a + row * Kf);
+            __nv_bfloat162* lo = (__nv_bfloat162*)((__nv_bfloat16*)feat_b + row * Kf);
+            const __nv_bfloat162 h = __floats2bfloat162_rn(a0, a1);
+            const float2 hf = __bfloat1622float2(h);
+            hi[col >> 1] = h;
+            lo[col >> 1] = __floats2bfloat162_rn(a0 - hf.x, a1 - hf.y);
+        } else {
+            float2* x = (float2*)((float*)feat_a + row * Kf);
+            x[col >> 1] = make_float2(a0, a1);
         }
     };
     // two consecutive slots per thread: they share a 64-wide chunk, so their feature columns
@@ -925,21 +961,34 @@ __global__ void __launch_bounds__(256) features_kernel(
         float f0[4], f1[4];
         feature(k, f0);
         feature(k + 1, f1);
-        const int64_t col = colmap[k];
-        if (MODE == 1) {
-            __nv_bfloat162* hi = (__nv_bfloat162*)((__nv_bfloat16*)feat_a + row * K4);
-            __nv_bfloat162* lo = (__nv_bfloat162*)((__nv_bfloat16*)feat_b + row * K4);
-#pragma unroll
-            for (int b = 0; b < 4; ++b) {
-                const __nv_bfloat162 h = __floats2bfloat162_rn(f0[b], f1[b]);
-                const float2 hf = __bfloat1622float2(h);
-                hi[(b * Kc_pad + col) >> 1] = h;
-                lo[(b * Kc_pad + col) >> 1] = __floats2bfloat162_rn(f0[b] - hf.x, f1[b] - hf.y);
-            }
-        } else {
-            float2* x = (float2*)((float*)feat_a + row * K4);
-#pragma unroll
-            for (int b = 0; b < 4; ++b) x[(b * Kc_pad + col) >> 1] = make_float2(f0[b], f1[b]);
+        const int64_t col = ft.colmap[k];
+        if (!RINGS) {
+            store2(col, f0[0], f1[0]);
+            store2(Kr_pad + col, f0[1], f1[1]);
+        }
+        store2(2 * Kr_pad + col, f0[2], f1[2]);
+        store2(2 * Kr_pad + Kc_pad + col, f0[3], f1[3]);
+    }
+    if (RINGS) {
+        __syncthreads();
+        // U(R) = sum of sw u' over the ring's members (in ring order), V(R) = C(m_R)^2 - mt(R)
+        auto ring = [&](int64_t R, float* U, float* V) {
+            *U = *V = 0.f;
+            if (R >= Kr) return;
+            const int b = ft.ring_start[R], e = ft.ring_start[R + 1];
+            float su = 0.f;
+            for (int i = b; i < e; ++i) su += tbuf[i];
+            int sg;
+            const float C = ctf_eval(ft.ring_m[R], qf, cc, &sg);
+            *U = su;
+            *V = (C * C - mu[4 * Kc_pad + R]) * sc;
+        };
+        for (int64_t R = 2 * (int64_t)threadIdx.x; R < Kr_pad; R += 512) {
+            float U0, V0, U1, V1;
+            ring(R, &U0, &V0);
+            ring(R + 1, &U1, &V1);
+            store2(R, U0, U1);
+            store2(Kr_pad + R, V0, V1);
         }
     }
     const double a = block_sum_double<256>((double)acc.value(), red);
@@ -1103,11 +1152,12 @@ int pd_sums(const mem_plan& P, const float2* spec, const uint64_t* qf, const Sum
 }
 
 int pd_finalize(const mem_plan& P, const float* partial, const SumItem* items,
-                const int32_t* item_off, const PdDev* pds, float* means, float2* avg_spec,
-                uint32_t* pd_max, int mode, cudaStream_t s) {
+                const int32_t* item_off, const PdDev* pds, const int32_t* ring_of, float* means,
+                float2* avg_spec, uint32_t* pd_max, int mode, cudaStream_t s) {
     if (mode & 2) MEM_CUDA_TRY(cudaMemsetAsync(pd_max, 0, sizeof(uint32_t) * P.n_pd, s));
     dim3 grid((unsigned)P.n_pd, (unsigned)((P.Kc_pad + 255) / 256));
-    pd_finalize_kernel<<<grid, 256, 0, s>>>(partial, items, item_off, pds, means, avg_spec,
+    pd_finalize_kernel<<<grid, 256, 0, s>>>(partial, items, item_off, pds,
+                                            P.ring_features ? ring_of : nullptr, means, avg_spec,
                                             pd_max, P.N, P.Nh, P.Kc, P.Kc_pad,
                                             means_stride(P), mode);
     MEM_LAUNCH_CHECK();
@@ -1115,20 +1165,30 @@ int pd_finalize(const mem_plan& P, const float* partial, const SumItem* items,
 }
 
 int features(const mem_plan& P, float2* spec, const uint64_t* qf, const PdDev* pds,
-             const int32_t* img_pd, const int32_t* img_row, const int32_t* colmap,
+             const int32_t* img_pd, const int32_t* img_row, const FeatTables& ft,
              const float* means, const uint32_t* scale_bits, void* feat_a, void* feat_b,
              double* pair_norm, float* ctf_out, float* spectrum_out, bool write_signed,
              cudaStream_t s) {
     if (P.n_images == 0) return MEM_OK;
-#define MEM_FEATS(MODE)                                                                        \
-    features_kernel<MODE><<<(unsigned)P.n_images, 256, 0, s>>>(                                \
-        spec, qf, pds, img_pd, img_row, colmap, means, scale_bits, feat_a, feat_b, pair_norm,  \
-        ctf_out, (float2*)spectrum_out, P.N, P.Nh, P.Kc, P.Kc_pad, means_stride(P), P.ctf,     \
-        write_signed ? 1 : 0)
-    if (P.params.precision == MEM_PREC_SPLIT_BF16)
-        MEM_FEATS(1);
-    else
-        MEM_FEATS(0);
+    const size_t smem = P.ring_features ? sizeof(float) * P.Kc : 0;
+#define MEM_FEATS(MODE, RINGS)                                                                 \
+    do {                                                                                       \
+        MEM_CUDA_TRY(cudaFuncSetAttribute(features_kernel<MODE, RINGS>,                        \
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize,         \
+                                          (int)smem));                                         \
+        features_kernel<MODE, RINGS><<<(unsigned)P.n_images, 256, smem, s>>>(                  \
+            spec, qf, pds, img_pd, img_row, ft, means, scale_bits, feat_a, feat_b, pair_norm,  \
+            ctf_out, (float2*)spectrum_out, P.N, P.Nh, P.Kc, P.Kc_pad, P.Kr, P.Kr_pad,         \
+            means_stride(P), P.ctf, write_signed ? 1 : 0);                                     \
+    } while (0)
+    const bool bf16 = P.params.precision == MEM_PREC_SPLIT_BF16;
+    if (P.ring_features) {
+        if (bf16) MEM_FEATS(1, true);
+        else MEM_FEATS(0, true);
+    } else {
+        if (bf16) MEM_FEATS(1, false);
+        else MEM_FEATS(0, false);
+    }
 #undef MEM_FEATS
     MEM_LAUNCH_CHECK();
     return MEM_OK;

@@ -60,9 +60,16 @@ def test_plan_tables_without_gpu(lib):
         assert lib.mem_plan_d_elements(h) == 300 ** 2 + 129 ** 2 + 1
         sz = ctypes.c_size_t()
         assert lib.mem_plan_workspace_size(h, ctypes.byref(sz)) == 0 and sz.value > 0
-        # the workspace holds at least the image, spectrum and feature buffers
-        Kc_pad = -(-64 * 33 // 64) * 64
-        assert sz.value >= 430 * 64 * 64 * 4 + 430 * 64 * 33 * 8 + (384 + 256 + 128) * 4 * Kc_pad * 4
+        # the workspace holds at least the image, spectrum and feature buffers; a feature row is
+        # [U' | V' | r' | s']: one U', V' column per ring of equal |k|^2, one r', s' column per
+        # half-plane frequency, each block padded to 64
+        pad = lambda x: -(-x // 64) * 64
+        ka = np.arange(64)[:, None]
+        kb = np.arange(33)[None, :]
+        rings = len(np.unique(np.minimum(ka, 64 - ka) ** 2 + kb ** 2))
+        Kf = 2 * pad(rings) + 2 * pad(64 * 33)
+        assert (rings, Kf) == (457, 5248)
+        assert sz.value >= 430 * 64 * 64 * 4 + 430 * 64 * 33 * 8 + (384 + 256 + 128) * Kf * 4
         small = ctypes.c_size_t(sz.value - 1)
         assert lib.mem_plan_upload(h, ctypes.c_void_p(256), small, None) == _lib.MEM_ERR_WORKSPACE
     finally:

@@ -139,3 +139,26 @@ def test_smem_fft_matches_cufft_path(cuda_ready, N):
         e = rel(np.asarray(outs[1][k]), np.asarray(outs[0][k]))
         print('N=%d %s: smem FFT vs cuFFT %.3g' % (N, k, e))
         assert e < 2e-6, (k, e)
+
+
+@pytest.mark.parametrize('precision', ['fp32', 'bf16x3'])
+@pytest.mark.parametrize('N', [64, 70, 128])
+def test_ring_features_match_per_frequency(cuda_ready, N, precision):
+    """Ring features (one U', V' column per ring of equal |k|^2) against per-frequency U', V'
+    blocks (MEM_RING_FEATURES=0): the same D within the contraction's precision, and against an
+    FP64 contraction of the GPU's spectra no worse than the per-frequency form."""
+    torch = cuda_ready
+    cfg, ds = _dataset(N, 150, near_dup=0.05, seed=90 + N)
+    res = {}
+    for ring in (0, 1):
+        res[ring] = _run(torch, cfg, ds, precision, env={'MEM_RING_FEATURES': ring})
+    e = rel(res[1]['D'], res[0]['D'])
+    D64 = _d64(cfg, ds, res[1])
+    e64 = rel(res[1]['D'], D64)
+    e64_pf = rel(res[0]['D'], _d64(cfg, ds, res[0]))
+    print('N=%d %s: ring vs per-frequency %.3g, vs FP64: ring %.3g, per-frequency %.3g'
+          % (N, precision, e, e64, e64_pf))
+    # no less accurate than the per-frequency layout (this PD has 5% near-duplicate images, so
+    # both forms sit near 1e-6 of the FP64 contraction at 128 px)
+    assert e < 2e-6 and e64 < max(1.25 * e64_pf, 1e-6)
+    np.testing.assert_array_equal(res[1]['D'], res[1]['D'].T)
