@@ -841,7 +841,7 @@ __global__ void __launch_bounds__(256) pd_finalize_kernel(
         av[k] = make_float2((float)(S[1] / wd / NN / n), (float)(S[2] / wd / NN / n));
     }
     if (!(mode & 2)) return;
-    const int kb = (int)(k % Nh);
+    const int kb = (int)k % Nh;
     const double w = (kb == 0 || (N % 2 == 0 && kb == N / 2)) ? 1.0 : 2.0;
     const double sw = sqrt(w), s2w = sqrt(2.0 * w);
     const float mu_u = (float)(sw * S[5] / n);
@@ -907,7 +907,8 @@ __global__ void __launch_bounds__(256) features_kernel(
     float2* sp = spec + img * Kc;
     KSum acc;
     auto weight = [&](int64_t k, int* m_out) {
-        const int ka = (int)(k / Nh), kb = (int)(k - (int64_t)ka * Nh);
+        const int kk = (int)k;                 // < Kc_pad: 32-bit division
+        const int ka = kk / Nh, kb = kk - ka * Nh;
         const int fa = min(ka, N - ka);
         *m_out = fa * fa + kb * kb;
         return (kb == 0 || ((N & 1) == 0 && kb == N / 2));     // half-plane weight 1
