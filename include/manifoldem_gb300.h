@@ -38,7 +38,7 @@ extern "C" {
 /* status codes */
 #define MEM_OK                    0
 #define MEM_ERR_INVALID          -1  /* bad argument (null pointer, size out of range)          */
-#define MEM_ERR_UNSUPPORTED      -2  /* box size or option this build does not support           */
+#define MEM_ERR_UNSUPPORTED      -2  /* box size or option this library does not support         */
 #define MEM_ERR_WORKSPACE        -3  /* workspace smaller than mem_plan_workspace_size()        */
 #define MEM_ERR_CUDA             -4  /* a CUDA runtime call failed                               */
 #define MEM_ERR_CUFFT            -5  /* a cuFFT call failed                                      */

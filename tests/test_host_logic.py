@@ -1,4 +1,5 @@
-"""Host-side logic of the driver: resume markers, job list, pickle format, HBM admission."""
+"""Host-side logic of the GetDistancesS2 replacement: resume markers, job list, pickle format,
+HBM admission."""
 import os
 import pickle
 import tempfile
