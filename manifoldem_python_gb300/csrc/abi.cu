@@ -371,6 +371,10 @@ int mem_plan_create(const mem_params* params, int32_t n_pd, const int32_t* pd_co
     if (const char* e = std::getenv("MEM_SMEM_FFT")) P->smem_fft = std::atoi(e) != 0;
     P->smem_fft = P->smem_fft && kern::smem_fft_supported(*P);
     if (const char* e = std::getenv("MEM_HOST_LOAD_CTAS")) P->host_load_ctas = std::atoi(e);
+    if (const char* e = std::getenv("MEM_HOST_LOAD_THREADS")) {
+        const int t = std::atoi(e);
+        if (t == 256 || t == 512 || t == 1024) P->host_load_threads = t;
+    }
 
     // cuFFT work sizes: exact when a device is current, an estimate otherwise
     std::vector<int> img_batches;

@@ -113,7 +113,10 @@ struct mem_plan {
     bool tc_kahan = false;          // compensated register sums across groups
     bool tc_lolo = false;           // add the lo.lo product (4-term split)
     bool smem_fft = true;           // shared-memory FFT kernels instead of cuFFT (N = 32, 64, 128)
-    int host_load_ctas = 128;       // grid of the host-to-device image copy of a split execute
+    // host-to-device image copy of a split execute: the fewer SMs it occupies the less it slows
+    // the concurrent computation; 24 x 1024 threads keep enough loads in flight for the link
+    int host_load_ctas = 24;
+    int host_load_threads = 1024;   // 256, 512 or 1024
                                     // with the stack in host memory
     bool timing = false;
     bool timed_run = false;

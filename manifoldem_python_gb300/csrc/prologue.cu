@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(NT) gather_normalize_kernel(
 
 // raw copy of every entry's stack image into slot i of out (a stack in host memory read over
 // the host link by a few light CTAs; the arithmetic then runs on the copies)
-__global__ void __launch_bounds__(256) gather_copy_kernel(
+__global__ void __launch_bounds__(1024) gather_copy_kernel(
         const float* __restrict__ stack, int64_t num_stack, const int64_t* __restrict__ sidx,
         int64_t n_images, int NN, float* __restrict__ out, uint32_t* __restrict__ status) {
     for (int64_t img = blockIdx.x; img < n_images; img += gridDim.x) {
@@ -1059,8 +1059,8 @@ int gather_copy(const mem_plan& P, const mem_inputs& in, float* out, uint32_t* s
                 int64_t ctas, cudaStream_t s) {
     if (P.n_images == 0) return MEM_OK;
     const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(ctas, P.n_images));
-    gather_copy_kernel<<<(unsigned)grid, 256, 0, s>>>(in.stack, in.num_stack, in.stack_index,
-                                                      P.n_images, P.N * P.N, out, status);
+    gather_copy_kernel<<<(unsigned)grid, P.host_load_threads, 0, s>>>(
+            in.stack, in.num_stack, in.stack_index, P.n_images, P.N * P.N, out, status);
     MEM_LAUNCH_CHECK();
     return MEM_OK;
 }
