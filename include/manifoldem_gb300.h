@@ -143,7 +143,7 @@ int mem_plan_execute(mem_plan* plan, const mem_inputs* in, const mem_outputs* ou
 /* mem_plan_execute with the reading of the stack issued on load_stream and the rest of the stage
  * on stream, which waits for it (an event owned by the plan).  With the stack in host memory
  * the load stream only copies the entries' images over the host link into free workspace
- * slots (24 CTAs of 1024 threads without shared memory, MEM_HOST_LOAD_CTAS /
+ * slots (8 CTAs of 1024 threads without shared memory, MEM_HOST_LOAD_CTAS /
  * MEM_HOST_LOAD_THREADS: few SMs, enough loads in flight for the link), so the loads of one plan
  * overlap the computation of other plans on other streams; a device-resident stack is read by
  * the first kernel of the stage on load_stream.  The reference has no counterpart (its workers

@@ -114,8 +114,9 @@ struct mem_plan {
     bool tc_lolo = false;           // add the lo.lo product (4-term split)
     bool smem_fft = true;           // shared-memory FFT kernels instead of cuFFT (N = 32, 64, 128)
     // host-to-device image copy of a split execute: the fewer SMs it occupies the less it slows
-    // the concurrent computation; 24 x 1024 threads keep enough loads in flight for the link
-    int host_load_ctas = 24;
+    // the concurrent computation; 8 x 1024 threads, two images per step, keep ~1 MB of loads in
+    // flight, enough for the host link
+    int host_load_ctas = 8;
     int host_load_threads = 1024;   // 256, 512 or 1024
                                     // with the stack in host memory
     bool timing = false;

@@ -117,23 +117,58 @@ __global__ void __launch_bounds__(NT) gather_normalize_kernel(
 __global__ void __launch_bounds__(1024) gather_copy_kernel(
         const float* __restrict__ stack, int64_t num_stack, const int64_t* __restrict__ sidx,
         int64_t n_images, int NN, float* __restrict__ out, uint32_t* __restrict__ status) {
-    for (int64_t img = blockIdx.x; img < n_images; img += gridDim.x) {
-        const int64_t s = sidx[img];
-        float* dst = out + img * (int64_t)NN;
-        if (s < 0 || s >= num_stack) {
-            if (threadIdx.x == 0) atomicOr(status, 2u);
-            for (int p = threadIdx.x; p < NN; p += blockDim.x) dst[p] = __int_as_float(0x7fc00000);
-            continue;
+    // two images per step (CTA images img and img + gridDim.x), their 16-byte loads issued
+    // before the stores, so that a small grid keeps enough reads in flight on the host link
+    const int64_t step = 2 * (int64_t)gridDim.x;
+    for (int64_t img = blockIdx.x; img < n_images; img += step) {
+        const int64_t img2 = img + gridDim.x;
+        const int n_img = img2 < n_images ? 2 : 1;
+        const float* src[2];
+        float* dst[2];
+        bool ok[2];
+        for (int q = 0; q < 2; ++q) {
+            const int64_t im = q == 0 ? img : img2;
+            const int64_t s = q < n_img ? sidx[im] : -1;
+            ok[q] = q < n_img && s >= 0 && s < num_stack;
+            src[q] = stack + (ok[q] ? s : 0) * (int64_t)NN;
+            dst[q] = out + im * (int64_t)NN;
+            if (q < n_img && !ok[q]) {
+                if (threadIdx.x == 0) atomicOr(status, 2u);
+                for (int p = threadIdx.x; p < NN; p += blockDim.x)
+                    dst[q][p] = __int_as_float(0x7fc00000);
+            }
         }
-        const float* src = stack + s * (int64_t)NN;
         if ((NN & 3) == 0) {
-            const float4* s4 = reinterpret_cast<const float4*>(src);
-            float4* d4 = reinterpret_cast<float4*>(dst);
-#pragma unroll 8
-            for (int p = threadIdx.x; p < NN / 4; p += blockDim.x) d4[p] = s4[p];
+            const int NQ = NN / 4;
+            const float4* s0 = reinterpret_cast<const float4*>(src[0]);
+            const float4* s1 = reinterpret_cast<const float4*>(src[1]);
+            float4* d0 = reinterpret_cast<float4*>(dst[0]);
+            float4* d1 = reinterpret_cast<float4*>(dst[1]);
+            for (int p0 = threadIdx.x; p0 < NQ; p0 += 4 * blockDim.x) {
+                float4 v[2][4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int p = p0 + u * blockDim.x;
+                    if (p < NQ) {
+                        if (ok[0]) v[0][u] = s0[p];
+                        if (ok[1]) v[1][u] = s1[p];
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int p = p0 + u * blockDim.x;
+                    if (p < NQ) {
+                        if (ok[0]) d0[p] = v[0][u];
+                        if (ok[1]) d1[p] = v[1][u];
+                    }
+                }
+            }
         } else {
+            for (int q = 0; q < 2; ++q) {
+                if (!ok[q]) continue;
 #pragma unroll 8
-            for (int p = threadIdx.x; p < NN; p += blockDim.x) dst[p] = src[p];
+                for (int p = threadIdx.x; p < NN; p += blockDim.x) dst[q][p] = src[q][p];
+            }
         }
     }
 }
