@@ -148,17 +148,19 @@ def test_dropin_op_writes_reference_pickle(cuda_ready):
     assert d['options'] == options
 
 
-@pytest.mark.parametrize('N', [64, 128, 192, 250])
+@pytest.mark.parametrize('N', [64, 128, 192, 250, 512])
 def test_box_sizes_match_oracle(cuda_ready, N):
     """Box sizes with their own kernels, against the FP64 oracle on a small PD with conjugate
     views: 64 and 128 px (shared-memory FFTs, compile-time-size rotation), the 192 px workload
-    size (cuFFT) and 250 px (rotation with global-memory coefficients)."""
+    size (cuFFT), 250 px (rotation with global-memory coefficients) and 512 px, the largest box
+    (per-frequency U', V' features: its half plane exceeds the ring-feature buffer)."""
     torch = cuda_ready
     import dataclasses
     from manifoldem_python_gb300.pipeline import DistanceStage, PdJob, StageParams
     from manifoldem_python_gb300.synthetic import CONFIGS, make_dataset
     from oracle import distance_oracle as O
-    cfg = dataclasses.replace(CONFIGS['config1'], N=N, n_fixed=8, conj_pd_frac=1.0, seed=60 + N)
+    cfg = dataclasses.replace(CONFIGS['config1'], N=N, n_fixed=8 if N < 512 else 5,
+                              conj_pd_frac=1.0, seed=60 + N)
     ds = make_dataset(cfg, device='cpu')
     ind = ds.CG[0]
     mic = dict(N=N, pix_size=cfg.pix, Cs=cfg.cs, EkV=cfg.kv, AmpContrast=cfg.ampc)
