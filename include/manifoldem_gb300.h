@@ -189,7 +189,7 @@ int mem_pd_batch(const mem_params* params, int32_t n_pd, const int32_t* pd_count
  *     current first); make that first call before any stream capture.
  *   - Sizes whose scratch (feature matrix rows padded to 128, spectra copy, sums) would exceed
  *     MEM_NOALLOC_SCRATCH_BYTES return MEM_ERR_TOO_LARGE without launching anything; at 128 px
- *     that allows n <= 128 images, at 70 px n <= 512; boxes above 177 px do not fit.
+ *     that allows n <= 187 images, at 70 px n <= 692; boxes above 220 px do not fit.
  *   - Every call on a device shares the one array and it keeps the last call's contents (the
  *     call re-initialises what it needs); calls that overlap on the GPU (other streams, other
  *     host threads) race on it and must be serialised by the caller.                          */

@@ -23,7 +23,7 @@ def _case(N, n, seed):
 
 
 @pytest.mark.parametrize('N,n,precision', [(64, 100, 'fp32'), (128, 120, 'fp32'),
-                                           (128, 120, 'bf16x3')])
+                                           (128, 187, 'bf16x3')])
 def test_noalloc_matches_plan_path_twice(cuda_ready, N, n, precision):
     torch = cuda_ready
     from manifoldem_python_gb300 import _lib
@@ -60,7 +60,8 @@ def test_noalloc_rejects_sizes_beyond_its_scratch(cuda_ready):
     lib = _lib.load()
     cp = StageParams(N=128, pix_size=2.0, Cs=2.7, EkV=300.0, AmpContrast=0.1).to_c()
     dummy = torch.zeros(16, dtype=torch.float64, device='cuda')
-    st = lib.mem_pd_distances_noalloc(ctypes.byref(cp), 2000, dummy.data_ptr(), dummy.data_ptr(),
-                                      dummy.data_ptr(), None)
-    assert st == _lib.MEM_ERR_TOO_LARGE
+    for n in (188, 2000):       # 187 images of 128 px are the most that fit
+        st = lib.mem_pd_distances_noalloc(ctypes.byref(cp), n, dummy.data_ptr(),
+                                          dummy.data_ptr(), dummy.data_ptr(), None)
+        assert st == _lib.MEM_ERR_TOO_LARGE, n
     assert 'static scratch' in _lib.status_string(st)
