@@ -210,3 +210,50 @@ def test_streamed_stage_matches_plain(cuda_ready):
         for a, b in zip(got, ref):
             for k in names:
                 np.testing.assert_array_equal(np.asarray(a[k]), np.asarray(b[k]))
+
+
+def _ellipsoid_mask(N):
+    """A binary mask volume: an off-centre ellipsoid (float32, (N, N, N), z y x)."""
+    z, y, x = np.meshgrid(*(np.arange(N, dtype=np.float64),) * 3, indexing='ij')
+    c = 0.5 * N
+    r = ((x - c - 2.) / (0.36 * N)) ** 2 + ((y - c + 1.) / (0.30 * N)) ** 2 + \
+        ((z - c) / (0.26 * N)) ** 2
+    return (r < 1).astype(np.float32)
+
+
+@pytest.mark.parametrize('N,branch', [(64, 'relion'), (128, 'relion'), (64, 'mask'),
+                                      (128, 'mask')])
+def test_relion_and_mask_box_sizes(cuda_ready, N, branch):
+    """The RELION read (order-3 'wrap' shift of the stored image) and the volume mask
+    (projectMask) at the shared-memory FFT sizes, against the FP64 oracle on a PD with conjugate
+    views (the golden fixtures pin both at 32 px against the reference itself)."""
+    torch = cuda_ready
+    import dataclasses
+    from manifoldem_python_gb300.pipeline import DistanceStage, PdJob, StageParams, VolumeMask
+    from manifoldem_python_gb300.synthetic import CONFIGS, make_dataset
+    from oracle import distance_oracle as O
+    cfg = dataclasses.replace(CONFIGS['config1'], N=N, n_fixed=12, conj_pd_frac=1.0,
+                              seed=80 + N + (0 if branch == 'relion' else 1))
+    ds = make_dataset(cfg, device='cpu')
+    ind = ds.CG[0]
+    mic = dict(N=N, pix_size=cfg.pix, Cs=cfg.cs, EkV=cfg.kv, AmpContrast=cfg.ampc)
+    stack = ds.stack.numpy()
+    sh = vol = None
+    if branch == 'relion':
+        rng = np.random.default_rng(N)
+        sh = (rng.uniform(-2.5, 2.5, stack.shape[0]), rng.uniform(-2.5, 2.5, stack.shape[0]))
+    else:
+        vol = _ellipsoid_mask(N)
+    ref = O.pd_op(ind, ds.q[:, ind], ds.df[ind], stack, ds.nStot, sh=sh, mask_volume=vol, **mic)
+    for precision in PRECISIONS:
+        mask = VolumeMask(vol) if vol is not None else None
+        res = DistanceStage(StageParams(precision=precision, **mic)).run(
+            [PdJob(ind=ind, q=ds.q[:, ind], df=ds.df[ind])], ds.stack.cuda(), ds.nStot,
+            sh=sh, mask=mask)[0]
+        if vol is not None:
+            np.testing.assert_array_equal(np.asarray(res['msk2']).reshape(N, N),
+                                          np.asarray(ref['msk2']).reshape(N, N))
+        for mk, rk in (('img_all', 'imgAll'), ('img_all_flip', 'imgAllFlip'),
+                       ('img_avg', 'imgAvg'), ('img_avg_flip', 'imgAvgFlip')):
+            assert rel(res[mk], ref[rk]) < TOL_IMG, (branch, N, mk, rel(res[mk], ref[rk]))
+        assert rel(res['D'], ref['D']) < 1e-5, (branch, N, rel(res['D'], ref['D']))
