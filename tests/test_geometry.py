@@ -28,3 +28,17 @@ def test_index_bookkeeping_conjugates():
     # odd nStot: the comparison is in floating point (ind < nStot/2)
     sidx, flip, lab = index_bookkeeping(np.array([2, 3]), 5)
     np.testing.assert_array_equal(flip, [0, 1])
+
+
+def test_empty_pd_raises_like_the_reference():
+    """An empty PD: the reference's op() fails in psi_ang (q2Spider's least-squares fit of a NaN
+    direction, getDistanceCTF_local_Conj9combinedS2.py:297-313) with scipy's ValueError; the
+    host geometry of the GPU stage fails the same way, before anything reaches the GPU."""
+    import warnings
+    import numpy as np
+    import pytest
+    from manifoldem_python_gb300.geometry import pd_geometry
+    with warnings.catch_warnings():
+        warnings.simplefilter('ignore', RuntimeWarning)
+        with pytest.raises(ValueError, match='not finite'):
+            pd_geometry(np.zeros(0, dtype=np.int64), np.zeros((4, 0)), 20)
