@@ -188,11 +188,28 @@ class PdJob:
     prD: int = 0
 
 
+RING_MAX_KC = 40960      # half planes up to this size use ring features (the library's kRingMaxKc)
+
+
+def feature_columns(N: int) -> int:
+    """Columns of a feature row: [U' | V' | r' | s'] with one U', V' column per ring of equal
+    |k|^2 (half planes up to RING_MAX_KC frequencies) or per frequency, each block padded to 64
+    (the library's feature_layout)."""
+    Nh = N // 2 + 1
+    Kc = N * Nh
+    pad = lambda x: -(-x // 64) * 64
+    if Kc <= RING_MAX_KC:
+        ka = np.arange(N)[:, None]
+        kb = np.arange(Nh)[None, :]
+        rings = int(np.unique(np.minimum(ka, N - ka) ** 2 + kb ** 2).size)
+        return 2 * pad(rings) + 2 * pad(Kc)
+    return 4 * pad(Kc)
+
+
 def workspace_bytes_per_image(params: StageParams) -> int:
     """Approximate device bytes one image needs (workspace and full outputs)."""
     N = params.N
-    Kc_pad = int(math.ceil(N * (N // 2 + 1) / 64.0) * 64)
-    feat = 4 * Kc_pad * 4
+    feat = 4 * feature_columns(N)          # FP32 features, or bf16 hi + lo
     return 4 * N * N * 4 + 8 * N * (N // 2 + 1) + feat + 64
 
 

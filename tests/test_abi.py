@@ -69,6 +69,8 @@ def test_plan_tables_without_gpu(lib):
         rings = len(np.unique(np.minimum(ka, 64 - ka) ** 2 + kb ** 2))
         Kf = 2 * pad(rings) + 2 * pad(64 * 33)
         assert (rings, Kf) == (457, 5248)
+        from manifoldem_python_gb300.pipeline import feature_columns
+        assert feature_columns(64) == Kf         # the batch-admission estimate's layout
         assert sz.value >= 430 * 64 * 64 * 4 + 430 * 64 * 33 * 8 + (384 + 256 + 128) * Kf * 4
         small = ctypes.c_size_t(sz.value - 1)
         assert lib.mem_plan_upload(h, ctypes.c_void_p(256), small, None) == _lib.MEM_ERR_WORKSPACE
