@@ -14,11 +14,13 @@ def init():
              eps=1e-10, img_stack_file='', align_param_file='', mask_vol_file='', num_part=0,
              Cs=2.7, EkV=300.0, AmpContrast=0.1, gaussEnv=np.inf, nPix=0, pix_size=1.0,
              PDsizeThL=100, PDsizeThH=2000, numberofJobs=0, tess_file='', dist_dir='',
-             dist_prog='', dist_file='')
+             dist_prog='', dist_file='', num_eigs=15, tune=3, rad=5, out_dir='', psi_dir='',
+             psi_prog='', psi_file='')
 
 
 def create_dir():
-    """Distance-stage directories under ``user_dir`` (reference p.py:116-123, :179)."""
+    """Distance-stage and diffusion-map directories under ``user_dir`` (reference
+    p.py:116-132, :179, :209)."""
     g = globals()
     g['dist_dir'] = os.path.join(user_dir, 'outputs_{}/distances/'.format(proj_name))
     os.makedirs(dist_dir, exist_ok=True)
@@ -26,6 +28,11 @@ def create_dir():
     os.makedirs(dist_prog, exist_ok=True)
     g['dist_file'] = '{}/IMGs_'.format(dist_dir)
     g['tess_file'] = os.path.join(user_dir, 'outputs_{}/selecGCs'.format(proj_name))
+    g['psi_dir'] = os.path.join(user_dir, 'outputs_{}/diff_maps/'.format(proj_name))
+    os.makedirs(psi_dir, exist_ok=True)
+    g['psi_prog'] = os.path.join(psi_dir, 'progress/')
+    os.makedirs(psi_prog, exist_ok=True)
+    g['psi_file'] = '{}/gC_trimmed_psi_'.format(psi_dir)
 
 
 def params_module():

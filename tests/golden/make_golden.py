@@ -251,10 +251,62 @@ def make_nlsa_case(name, seed=5):
     print('wrote', path, os.path.getsize(path) // 1024, 'KiB')
 
 
+# Manifold trimming cases: the reference's manifoldTrimmingAuto.op (modules/
+# manifoldTrimmingAuto.py:38-95) as manifoldAnalysis.op calls it (:81-99: posPath 0, tune 3,
+# visual False, doSave Is True) on the reference's D of an earlier fixture, written to a distance
+# pickle first.  rad 5 is the default (p.py:77); rad 3 makes the trimming loop run.  np.random
+# is seeded before each run.  Stored: the psi pickle's arrays and the eigenvalue file's text.
+TRIM_CASES = {
+    'trim_config1': dict(source='config1', rads=(5.0, 3.0), seed=0),
+    'trim_nlsa32': dict(source='nlsa32', rads=(3.0,), seed=0),
+}
+TRIM_KEYS = ['lamb', 'psi', 'sigma', 'mu', 'posPath', 'ind', 'logEps', 'logSumWij', 'popt',
+             'R_squared']
+
+
+def make_trim_case(name):
+    spec = TRIM_CASES[name]
+    ref_p, _ = load_reference()
+    ref_p.init()
+    sys.modules.setdefault('h5py', types.ModuleType('h5py'))
+    import manifoldTrimmingAuto                         # noqa: E402
+    import myio                                         # noqa: E402
+    src = np.load(os.path.join(HERE, spec['source'] + '.npz'))
+    D = np.asarray(src['ref_D'] if 'ref_D' in src.files else src['D'], dtype=np.float64)
+    ind = np.asarray(src['ind']) if 'ind' in src.files else np.arange(D.shape[0])
+    # D itself stays in the source fixture
+    rec = dict(source=np.array(spec['source']), ind=ind, rads=np.array(spec['rads']),
+               seed=np.int64(spec['seed']))
+    with tempfile.TemporaryDirectory() as tmp:
+        ref_p.psi_prog = os.path.join(tmp, 'progress')
+        os.makedirs(ref_p.psi_prog)
+        dist_file = os.path.join(tmp, 'IMGs_prD_0')
+        myio.fout1(dist_file, ['D', 'ind'], [D, ind])
+        for r, rad in enumerate(spec['rads']):
+            psi_file = os.path.join(tmp, 'psi_%d' % r)
+            eig_file = os.path.join(tmp, 'eig_%d.txt' % r)
+            np.random.seed(spec['seed'])
+            manifoldTrimmingAuto.op([dist_file, psi_file, eig_file, 0], 0, 3, rad, False,
+                                    dict(outputFile='', Is=True))
+            with open(psi_file, 'rb') as fh:
+                out = pickle.load(fh)
+            for key in TRIM_KEYS:
+                if key != 'ind':
+                    rec['r%d_%s' % (r, key)] = np.asarray(out[key])
+            with open(eig_file) as fh:
+                rec['r%d_eig_txt' % r] = np.array(fh.read())
+            print(name, 'rad', rad, 'kept', len(out['posPath']), 'of', D.shape[0])
+    path = os.path.join(HERE, name + '.npz')
+    np.savez_compressed(path, **rec)
+    print('wrote', path, os.path.getsize(path) // 1024, 'KiB')
+
+
 if __name__ == '__main__':
-    names = sys.argv[1:] or list(CASES) + list(NLSA_CASES)
+    names = sys.argv[1:] or list(CASES) + list(NLSA_CASES) + list(TRIM_CASES)
     for n in names:
         if n in NLSA_CASES:
             make_nlsa_case(n)
+        elif n in TRIM_CASES:
+            make_trim_case(n)
         else:
             make_case(n)
