@@ -492,7 +492,7 @@ __global__ void __launch_bounds__(NT) rotate_kernel(
 // Compile-time box size (power-of-two N, 512 threads): the same computation as rotate_kernel
 // with every loop bound, row stride and tap offset a constant, the tap indices wrapped by a
 // mask, the -1 of the 4-tap window folded into the fixed-point origin and the prefilter
-// recursions unrolled.  Segment start sums use kInitTaps taps (N >= kInitTaps).
+// segments held in registers (prefilter_fixed).
 // Row stride of the coefficient image in the compile-time kernels: >= N + 3 (halo) and = 1 mod 32,
 // so that the bank of tap (ix, iy) is (ix + iy) mod 32; a warp's 32 samples along a line whose
 // direction has components of one sign then meet at most about two to a bank.
@@ -501,76 +501,77 @@ __host__ __device__ constexpr int rot_stride() {
     return ((N + 3 + 30) / 32) * 32 + 1;
 }
 
+template <int NT, int N>
+__host__ __device__ constexpr int rot_nseg() {
+    return (NT / N < N / 8) ? NT / N : N / 8;
+}
+
+template <int K>
+__device__ constexpr float z1_pow() {
+    float p = 1.f;
+    for (int i = 0; i < K; ++i) p *= kZ1;
+    return p;
+}
+
+// The periodic cubic B-spline prefilter along one axis, with each line split into NSEG segments
+// of SEG >= 8 samples, one thread per segment holding it in registers.  Causal pass
+// c+[k] = x[k] + z1 c+[k-1]: the thread first forms its segment's end state from zero,
+// E = sum_k z1^(SEG-1-k) x[k]; the state entering segment g is sum_m z1^(SEG (m-1)) E[g-m] over
+// the CT = ceil(32 / SEG) previous segments (the rest of the periodic sum is below
+// z1^32 = 5e-19 of it); the recursion then runs from that state.  The anticausal pass c-[k] = c+[k] + z1 c-[k+1] does the
+// same from the segment's end, and the output is -6 z1 c-[k].  Each sample is read and written
+// once; segment states go through carry[] (2 NSEG N floats).
 template <int NT, int N, int AXIS>
-__device__ __forceinline__ void prefilter_fixed(float* s) {
+__device__ __forceinline__ void prefilter_fixed(float* s, float* carry) {
     constexpr int P = rot_stride<N>();
-    constexpr int NSEG = (NT / N < N / 16) ? NT / N : N / 16;
+    constexpr int NSEG = rot_nseg<NT, N>();
     constexpr int SEG = N / NSEG, LINES = N * NSEG;
+    constexpr int CT = (32 + SEG - 1) / SEG;
+    static_assert(SEG >= 8 && N % NSEG == 0, "segments of at least 8 samples");
     constexpr int SK = AXIS == 0 ? 1 : P, SL = AXIS == 0 ? P : 1;
+    constexpr float zseg = z1_pow<SEG>();
+    constexpr float gain = -6.0f * kZ1;
     const int t = threadIdx.x;
-    const bool active = t < LINES;
+    const bool active = LINES >= NT || t < LINES;     // a constant when every thread has a segment
     const int line = t % N, g = t / N;
-    const int k0 = g * SEG, k1 = k0 + SEG - 1;
-    float* base = s + line * SL;
-    float init = 0.f;
+    float* b0 = s + line * SL + g * SEG * SK;
+    float* carry_c = carry;                 // [NSEG][N] causal end states
+    float* carry_a = carry + NSEG * N;      // [NSEG][N] anticausal start states
+    float v[SEG];
     if (active) {
-        float acc = 0.f, zp = 1.f;
-        if (k0 < kInitTaps - 1) {            // the taps wrap around the line's start
+        float e = 0.f;
 #pragma unroll
-            for (int j = 0; j < kInitTaps; ++j) {
-                acc += zp * base[((k0 - j) & (N - 1)) * SK];
-                zp *= kZ1;
-            }
-        } else {
-            const float* b0 = base + k0 * SK;
-#pragma unroll
-            for (int j = 0; j < kInitTaps; ++j) {
-                acc += zp * b0[-j * SK];
-                zp *= kZ1;
-            }
+        for (int k = 0; k < SEG; ++k) {
+            v[k] = b0[k * SK];
+            e = fmaf(kZ1, e, v[k]);
         }
-        init = acc;
+        carry_c[g * N + line] = e;
     }
     __syncthreads();
     if (active) {
-        float* b0 = base + k0 * SK;
-        float prev = init;
-        b0[0] = prev;
+        float c = 0.f;
 #pragma unroll
-        for (int k = 1; k < SEG; ++k) {
-            prev = b0[k * SK] + kZ1 * prev;
-            b0[k * SK] = prev;
+        for (int m = CT; m >= 1; --m)
+            c = fmaf(zseg, c, carry_c[((g + CT * NSEG - m) % NSEG) * N + line]);
+#pragma unroll
+        for (int k = 0; k < SEG; ++k) {
+            c = fmaf(kZ1, c, v[k]);
+            v[k] = c;
         }
+        float e = 0.f;
+#pragma unroll
+        for (int k = SEG - 1; k >= 0; --k) e = fmaf(kZ1, e, v[k]);
+        carry_a[g * N + line] = e;
     }
     __syncthreads();
     if (active) {
-        float acc = 0.f, zp = 1.f;
-        if (k1 + kInitTaps - 1 >= N) {       // the taps wrap around the line's end
+        float c = 0.f;
 #pragma unroll
-            for (int j = 0; j < kInitTaps; ++j) {
-                acc += zp * base[((k1 + j) & (N - 1)) * SK];
-                zp *= kZ1;
-            }
-        } else {
-            const float* b1 = base + k1 * SK;
+        for (int m = CT; m >= 1; --m) c = fmaf(zseg, c, carry_a[((g + m) % NSEG) * N + line]);
 #pragma unroll
-            for (int j = 0; j < kInitTaps; ++j) {
-                acc += zp * b1[j * SK];
-                zp *= kZ1;
-            }
-        }
-        init = acc;
-    }
-    __syncthreads();
-    if (active) {
-        constexpr float gain = -6.0f * kZ1;
-        float* b0 = base + k0 * SK;
-        float prev = init;
-        b0[(SEG - 1) * SK] = gain * prev;
-#pragma unroll
-        for (int k = SEG - 2; k >= 0; --k) {
-            prev = b0[k * SK] + kZ1 * prev;
-            b0[k * SK] = gain * prev;
+        for (int k = SEG - 1; k >= 0; --k) {
+            c = fmaf(kZ1, c, v[k]);
+            b0[k * SK] = gain * c;
         }
     }
     __syncthreads();
@@ -653,6 +654,7 @@ __global__ void __launch_bounds__(NT, 2) rotate_fixed_kernel(
     constexpr int P = rot_stride<N>(), NN = N * N, R = NT / N, MAXV = N / R;
     extern __shared__ float s[];
     __shared__ RotConst rot[2];
+    __shared__ float carry[2 * rot_nseg<NT, N>() * N];
     const int64_t img = blockIdx.x;
     float* xi = xbuf + img * (int64_t)NN;
     if (threadIdx.x == 0) {
@@ -669,8 +671,8 @@ __global__ void __launch_bounds__(NT, 2) rotate_fixed_kernel(
     __syncthreads();
 #pragma unroll 1
     for (int pass = 0; pass < 2; ++pass) {
-        prefilter_fixed<NT, N, 0>(s);
-        prefilter_fixed<NT, N, 1>(s);
+        prefilter_fixed<NT, N, 0>(s, carry);
+        prefilter_fixed<NT, N, 1>(s, carry);
         fill_halo<NT>(s, N, P);
         float keep[MAXV];
         int base, stride;
