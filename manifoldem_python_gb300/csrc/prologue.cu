@@ -783,13 +783,37 @@ __global__ void qfix_kernel(const double* __restrict__ df, uint64_t* __restrict_
     qfix[i] = (v >= 18446744073709551615.0) ? 0ull : __double2ull_rn(v);
 }
 
+// sin(2 pi u / 2^64) of a phase u in 64-bit fixed-point cycles.  The top three bits give the
+// octant o; the next 32 give y in [0, 1) (mirrored to 1 - y in odd octants), so that the value
+// is +-sin(pi y / 4) (o mod 4 = 0, 3) or +-cos(pi y / 4) (o mod 4 = 1, 2), negative for o >= 4.
+// Both are polynomials in y fitted here (weighted least squares on the relative error, each
+// coefficient rounded to float in turn with the later ones refitted): max error 1.6 ulp (sin)
+// and 0.9 ulp (cos) on [0, 1] in float arithmetic with fused multiply-adds; the float y adds at
+// most pi/4 * 2^-24 = 4.7e-8 to the argument.
+__device__ __forceinline__ float sin_cycles(uint64_t u) {
+    const uint32_t o = (uint32_t)(u >> 61);
+    uint32_t t = (uint32_t)(u >> 29);
+    if (o & 1u) t = ~t;
+    const float y = (float)t * 2.3283064365386963e-10f;     // t / 2^32
+    const float y2 = y * y;
+    float ps = fmaf(y2, -3.661072696559131e-05f, 0.0024910178035497665f);
+    ps = fmaf(y2, ps, -0.08074583113193512f);
+    ps = fmaf(y2, ps, 0.7853981852531433f);
+    ps *= y;                                                // sin(pi y / 4)
+    float pc = fmaf(y2, 3.4940505884151207e-06f, -0.0003258686629123986f);
+    pc = fmaf(y2, pc, 0.015854284167289734f);
+    pc = fmaf(y2, pc, -0.3084251284599304f);
+    pc = fmaf(y2, pc, 1.0f);                                // cos(pi y / 4)
+    const float v = ((o + 1u) & 2u) ? pc : ps;
+    return (o & 4u) ? -v : v;
+}
+
 __device__ __forceinline__ float ctf_eval(int m, uint64_t qf, const CtfConst& cc, int* sgn) {
     const uint64_t mm = (uint64_t)m;
     const uint64_t ph = cc.p_fix * (mm * mm) - qf * mm - cc.d_fix;
     const int64_t sph = (int64_t)ph;
     *sgn = (sph > 0) - (sph < 0);
-    const float cyc = (float)sph * 5.421010862427522e-20f;   // 2^-64
-    float v = cc.amp * sinpif(2.0f * cyc);
+    float v = cc.amp * sin_cycles(ph);
     if (cc.env_c != 0.0f) v *= expf(-cc.env_c * (float)m);
     return v;
 }
