@@ -27,6 +27,20 @@ __device__ __forceinline__ float mask_ref(int r, int c, int N) {
     return (x * x + y * y < h * h) ? 1.0f : 0.0f;
 }
 
+// Two Kahan-compensated float sums in paired FP32 instructions (fadd.rn.f32x2 / fma.rn.f32x2),
+// the compensation kept negated, e = -c: y = x + e, t = s + y, e = (s - t) + y, s = t -- the
+// same roundings as KSum below, so the sums are bit-identical to two KSum.
+struct KSum2 {
+    float2 s = make_float2(0.f, 0.f), e = make_float2(0.f, 0.f);
+    __device__ __forceinline__ void add(float2 x) {
+        const float2 y = __fadd2_rn(x, e);
+        const float2 t = __fadd2_rn(s, y);
+        e = __fadd2_rn(__ffma2_rn(t, make_float2(-1.f, -1.f), s), y);
+        s = t;
+    }
+    __device__ __forceinline__ float2 value() const { return __fadd2_rn(s, e); }
+};
+
 // Kahan-compensated float accumulator
 struct KSum {
     float s = 0.f, c = 0.f;
@@ -834,35 +848,36 @@ __global__ void __launch_bounds__(256) pd_sums_kernel(
         const int ka = (int)(k / Nh), kb = (int)(k - (int64_t)ka * Nh);
         const int fa = min(ka, N - ka);
         const int m = fa * fa + kb * kb;
-        KSum s0, s1, s2, s3, s4, s5;
+        KSum2 s05, s12, s34;        // (S0, S5), (S1, S2), (S3, S4)
 #pragma unroll 4
         for (int64_t i = it.img_begin; i < it.img_end; ++i) {
             const float2 F = spec[i * Kc + k];
             int sg;
+            float C = 0.f;
             if (WHICH & 1) {
-                const float C = ctf_eval(m, qfix[i], cc, &sg);
-                s0.add(C * C);
-                s1.add(C * F.x);
-                s2.add(C * F.y);
+                C = ctf_eval(m, qfix[i], cc, &sg);
+                s12.add(__fmul2_rn(make_float2(C, C), F));
             } else {
                 sg = ctf_sign(m, qfix[i], cc);
             }
             if (WHICH & 2) {
-                s3.add(sg > 0 ? F.x : (sg < 0 ? -F.x : 0.f));
-                s4.add(sg > 0 ? F.y : (sg < 0 ? -F.y : 0.f));
-                s5.add(F.x * F.x + F.y * F.y);
+                const float g = (float)sg;
+                s34.add(__fmul2_rn(make_float2(g, g), F));
             }
+            s05.add(make_float2((WHICH & 1) ? C * C : 0.f,
+                                (WHICH & 2) ? F.x * F.x + F.y * F.y : 0.f));
         }
         float* out = partial + (int64_t)blockIdx.x * 6 * Kc + k;
+        const float2 v05 = s05.value(), v12 = s12.value(), v34 = s34.value();
         if (WHICH & 1) {
-            out[0 * Kc] = s0.value();
-            out[1 * Kc] = s1.value();
-            out[2 * Kc] = s2.value();
+            out[0 * Kc] = v05.x;
+            out[1 * Kc] = v12.x;
+            out[2 * Kc] = v12.y;
         }
         if (WHICH & 2) {
-            out[3 * Kc] = s3.value();
-            out[4 * Kc] = s4.value();
-            out[5 * Kc] = s5.value();
+            out[3 * Kc] = v34.x;
+            out[4 * Kc] = v34.y;
+            out[5 * Kc] = v05.y;
         }
     }
 }
