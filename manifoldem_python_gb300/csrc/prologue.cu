@@ -969,7 +969,8 @@ __global__ void __launch_bounds__(256) features_kernel(
         const uint32_t* __restrict__ scale_bits, void* __restrict__ feat_a, void* __restrict__ feat_b,
         double* __restrict__ pair_norm, float* __restrict__ ctf_out,
         float2* __restrict__ spectrum_out, int N, int Nh, int64_t Kc, int64_t Kc_pad,
-        int64_t Kr, int64_t Kr_pad, int64_t mstride, CtfConst cc, int write_signed) {
+        int64_t Kr, int64_t Kr_pad, int64_t mstride, CtfConst cc, int write_signed,
+        int pair_loads) {
     __shared__ double red[32];
     extern __shared__ float tbuf[];          // RINGS: sw u' of every frequency (scaled)
     const int64_t img = blockIdx.x;
@@ -1019,6 +1020,54 @@ __global__ void __launch_bounds__(256) features_kernel(
             sp[k] = make_float2(sgf * F.x, sgf * F.y);
         }
     };
+    // slots k, k + 1 (k even, k + 1 < Kc) with paired FP32 instructions and 16-byte spectrum /
+    // 8-byte centring-vector loads (pair_loads: Kc even, so both are aligned); the same
+    // operations per element as feature(), the a_i terms summed in a second compensated pair
+    KSum2 acc2;
+    auto feature_pair = [&](int64_t k, float (&f0)[4], float (&f1)[4]) {
+        const float2 m1 = make_float2(-1.f, -1.f);
+        auto sub2 = [&](float2 a, float2 b) { return __ffma2_rn(b, m1, a); };     // a - b
+        int m0, mb;
+        const bool w0 = weight(k, &m0), wb = weight(k + 1, &mb);
+        const float2 sw = make_float2(w0 ? 1.0f : 1.41421356237309505f,
+                                      wb ? 1.0f : 1.41421356237309505f);
+        const float2 s2w = make_float2(w0 ? 1.41421356237309505f : 2.0f,
+                                       wb ? 1.41421356237309505f : 2.0f);
+        const float4 FF = *reinterpret_cast<const float4*>(sp + k);
+        if (spectrum_out) *reinterpret_cast<float4*>(spectrum_out + img * Kc + k) = FF;
+        int sg0, sg1;
+        const float2 C = make_float2(ctf_eval(m0, qf, cc, &sg0), ctf_eval(mb, qf, cc, &sg1));
+        const float2 Fx = make_float2(FF.x, FF.z), Fy = make_float2(FF.y, FF.w);
+        const float2 u = __fmul2_rn(sw, __ffma2_rn(Fx, Fx, __fmul2_rn(Fy, Fy)));
+        const float2 v = __fmul2_rn(sw, __fmul2_rn(C, C));
+        const float2 q = __fmul2_rn(s2w, C);
+        const float2 r = __fmul2_rn(q, Fx), sv = __fmul2_rn(q, Fy);
+        const float2 mu_u = *reinterpret_cast<const float2*>(mu + k);
+        const float2 mu_v = *reinterpret_cast<const float2*>(mu + Kc_pad + k);
+        const float2 mu_r = *reinterpret_cast<const float2*>(mu + 2 * Kc_pad + k);
+        const float2 mu_s = *reinterpret_cast<const float2*>(mu + 3 * Kc_pad + k);
+        const float2 half = make_float2(0.5f, 0.5f);
+        // mu_u (v - mu_v) + mu_v u + mu_r (mu_r / 2 - r) + mu_s (mu_s / 2 - s)
+        float2 a = __fmul2_rn(mu_u, sub2(v, mu_v));
+        a = __ffma2_rn(mu_v, u, a);
+        a = __ffma2_rn(mu_r, sub2(__fmul2_rn(half, mu_r), r), a);
+        a = __ffma2_rn(mu_s, sub2(__fmul2_rn(half, mu_s), sv), a);
+        acc2.add(a);
+        const float2 scv = make_float2(sc, sc);
+        const float2 fu = __fmul2_rn(sub2(u, mu_u), scv), fv = __fmul2_rn(sub2(v, mu_v), scv);
+        const float2 fr = __fmul2_rn(sub2(r, mu_r), scv), fs = __fmul2_rn(sub2(sv, mu_s), scv);
+        f0[0] = fu.x, f0[1] = fv.x, f0[2] = fr.x, f0[3] = fs.x;
+        f1[0] = fu.y, f1[1] = fv.y, f1[2] = fr.y, f1[3] = fs.y;
+        if (RINGS) {
+            tbuf[ft.pos_of[k]] = sw.x * fu.x;
+            tbuf[ft.pos_of[k + 1]] = sw.y * fu.y;
+        }
+        if (write_signed) {
+            const float g0 = (float)sg0 * inv_nn, g1 = (float)sg1 * inv_nn;
+            *reinterpret_cast<float4*>(sp + k) =
+                make_float4(g0 * FF.x, g0 * FF.y, g1 * FF.z, g1 * FF.w);
+        }
+    };
     auto store2 = [&](int64_t col, float a0, float a1) {     // columns col, col + 1 (col even)
         if (MODE == 1) {
             __nv_bfloat162* hi = (__nv_bfloat162*)((__nv_bfloat16*)feat_a + row * Kf);
@@ -1036,8 +1085,12 @@ __global__ void __launch_bounds__(256) features_kernel(
     // are adjacent (col even) and each block gets one paired store
     for (int64_t k = 2 * (int64_t)threadIdx.x; k < Kc_pad; k += 512) {
         float f0[4], f1[4];
-        feature(k, f0);
-        feature(k + 1, f1);
+        if (pair_loads && k < Kc) {
+            feature_pair(k, f0, f1);
+        } else {
+            feature(k, f0);
+            feature(k + 1, f1);
+        }
         const int64_t col = ft.colmap[k];
         if (!RINGS) {
             store2(col, f0[0], f1[0]);
@@ -1068,7 +1121,9 @@ __global__ void __launch_bounds__(256) features_kernel(
             store2(Kr_pad + R, V0, V1);
         }
     }
-    const double a = block_sum_double<256>((double)acc.value(), red);
+    const float2 a2 = acc2.value();
+    const double a = block_sum_double<256>((double)acc.value() + (double)a2.x + (double)a2.y,
+                                           red);
     if (threadIdx.x == 0) pair_norm[img] = a;
     if (ctf_out) {
         float* co = ctf_out + img * (int64_t)N * N;
@@ -1256,7 +1311,7 @@ int features(const mem_plan& P, float2* spec, const uint64_t* qf, const PdDev* p
         features_kernel<MODE, RINGS><<<(unsigned)P.n_images, 256, smem, s>>>(                  \
             spec, qf, pds, img_pd, img_row, ft, means, scale_bits, feat_a, feat_b, pair_norm,  \
             ctf_out, (float2*)spectrum_out, P.N, P.Nh, P.Kc, P.Kc_pad, P.Kr, P.Kr_pad,         \
-            means_stride(P), P.ctf, write_signed ? 1 : 0);                                     \
+            means_stride(P), P.ctf, write_signed ? 1 : 0, P.Kc % 2 == 0 ? 1 : 0);              \
     } while (0)
     const bool bf16 = P.params.precision == MEM_PREC_SPLIT_BF16;
     if (P.ring_features) {
