@@ -71,17 +71,37 @@ struct KSumF {
     __device__ __forceinline__ float value() const { return s - c; }
 };
 
+// background mean and 1/std of an image of NN pixels from per-thread partial sums a (values)
+// and b (squares), red[2 NT / 32]: warp sums in FP64, then one thread adds the warp sums and
+// forms the mean and 1/std (FP64 arithmetic is slow on this part; the other threads take the
+// results from shared memory instead of repeating it)
 template <int NT>
-__device__ __forceinline__ double block_sum(double v, double* red) {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+__device__ __forceinline__ void block_stats(double a, double b, double* red, int NN,
+                                            float* mean, float* inv) {
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
     __syncthreads();
-    if (l == 0) red[w] = v;
+    if (l == 0) {
+        red[w] = a;
+        red[NT / 32 + w] = b;
+    }
     __syncthreads();
-    double t = 0.0;
+    if (threadIdx.x == 0) {
+        double t = 0.0, t2 = 0.0;
 #pragma unroll
-    for (int i = 0; i < NT / 32; ++i) t += red[i];
-    return t;
+        for (int i = 0; i < NT / 32; ++i) t += red[i];
+#pragma unroll
+        for (int i = 0; i < NT / 32; ++i) t2 += red[NT / 32 + i];
+        const double m = t / NN;
+        red[0] = m;
+        red[1] = 1.0 / sqrt(fmax(t2 / NN - m * m, 0.0));
+    }
+    __syncthreads();
+    *mean = (float)red[0];
+    *inv = (float)red[1];
 }
 
 // The stages of the transform.  Thread mapping: warp w owns pair-rows and columns 8w..8w+7;
@@ -459,11 +479,9 @@ __device__ __forceinline__ void lowpass_image(
             S[F::addr(p, b)] = make_float2(x0, x1);
         }
     }
-    const double tot = block_sum<NT>((double)sum.value(), red);
-    const double tot2 = block_sum<NT>((double)sq.value(), red);
-    const double mean = tot / NN;
-    const float inv = (float)(1.0 / sqrt(fmax(tot2 / NN - mean * mean, 0.0)));
-    F::template rows_forward<true>(S, W, (float)mean, inv);
+    float mean, inv;
+    block_stats<NT>((double)sum.value(), (double)sq.value(), red, NN, &mean, &inv);
+    F::template rows_forward<true>(S, W, mean, inv);
     __syncthreads();
     F::cols_forward1(S, W);
     __syncwarp();
@@ -483,7 +501,7 @@ __global__ void __launch_bounds__(2 * N, N == 128 ? 2 : 4) lowpass_fft_kernel(
     using F = Fft2<N>;
     extern __shared__ float2 S[];                      // [N/2][N], swizzled
     __shared__ float2 W[N];
-    __shared__ double red[F::NT / 32];
+    __shared__ double red[2 * (F::NT / 32)];
     F::twiddles(W, twid);
     lowpass_image<N>(blockIdx.x, S, W, red, stack, num_stack, sidx, flip, gtab, xbuf, status);
 }

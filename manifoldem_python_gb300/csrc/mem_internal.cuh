@@ -55,7 +55,7 @@ struct CtfConst {
 // sign of the 64-bit fixed-point phase P m^2 - Q m - atan(A)/2pi, whose sine (times a positive
 // amplitude) is the CTF
 __device__ __forceinline__ int ctf_sign(int m, uint64_t qf, const CtfConst& cc) {
-    const uint64_t mm = (uint64_t)m;
+    const uint64_t mm = (uint32_t)m;                  // m >= 0: zero-extended
     const int64_t sph = (int64_t)(cc.p_fix * (mm * mm) - qf * mm - cc.d_fix);
     return (sph > 0) - (sph < 0);
 }

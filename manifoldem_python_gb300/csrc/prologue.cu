@@ -53,6 +53,39 @@ struct KSum {
     __device__ __forceinline__ float value() const { return s - c; }
 };
 
+// background mean and 1/std of an image of NN pixels from per-thread partial sums a (values)
+// and b (squares), red[2 NT / 32]: warp sums in FP64, then one thread adds the warp sums and
+// forms the mean and 1/std (FP64 arithmetic is slow on this part; the other threads take the
+// results from shared memory instead of repeating it)
+template <int NT>
+__device__ __forceinline__ void block_stats(double a, double b, double* red, int NN,
+                                            float* mean, float* inv) {
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) {
+        red[w] = a;
+        red[NT / 32 + w] = b;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0, t2 = 0.0;
+#pragma unroll
+        for (int i = 0; i < NT / 32; ++i) t += red[i];
+#pragma unroll
+        for (int i = 0; i < NT / 32; ++i) t2 += red[NT / 32 + i];
+        const double m = t / NN;
+        red[0] = m;
+        red[1] = 1.0 / sqrt(fmax(t2 / NN - m * m, 0.0));
+    }
+    __syncthreads();
+    *mean = (float)red[0];
+    *inv = (float)red[1];
+}
+
 template <int NT>
 __device__ __forceinline__ double block_sum_double(double v, double* red) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -101,12 +134,9 @@ __device__ __forceinline__ void gather_normalize_one(
         sum.add(bg);
         sq.add(bg * bg);
     }
-    const double tot = block_sum_double<NT>((double)sum.value(), red);
-    const double tot2 = block_sum_double<NT>((double)sq.value(), red);
-    const double mean = tot / NN;
-    const double var = fmax(tot2 / NN - mean * mean, 0.0);
-    const float fmean = (float)mean;
-    const float inv = (float)(1.0 / sqrt(var));
+    static_assert(NT <= 512, "red[32] holds two sets of warp sums");
+    float fmean, inv;
+    block_stats<NT>((double)sum.value(), (double)sq.value(), red, NN, &fmean, &inv);
     for (int p = threadIdx.x; p < NN; p += NT) {
         const int a = p / N, b = p - a * N;
         dst[p] = (src[a * N + (f ? N - 1 - b : b)] - fmean) * inv;
@@ -225,12 +255,9 @@ __device__ __forceinline__ void gather_normalize_v4_one(
             sq.add(bg * bg);
         }
     }
-    const double tot = block_sum_double<NT>((double)sum.value(), red);
-    const double tot2 = block_sum_double<NT>((double)sq.value(), red);
-    const double mean = tot / NN;
-    const double var = fmax(tot2 / NN - mean * mean, 0.0);
-    const float fmean = (float)mean;
-    const float inv = (float)(1.0 / sqrt(var));
+    static_assert(NT <= 512, "red[32] holds two sets of warp sums");
+    float fmean, inv;
+    block_stats<NT>((double)sum.value(), (double)sq.value(), red, NN, &fmean, &inv);
     for (int p = threadIdx.x; p < NQ; p += NT) {
         int a, b;
         const float4 v = load(p, a, b);
@@ -823,7 +850,7 @@ __device__ __forceinline__ float sin_cycles(uint64_t u) {
 }
 
 __device__ __forceinline__ float ctf_eval(int m, uint64_t qf, const CtfConst& cc, int* sgn) {
-    const uint64_t mm = (uint64_t)m;
+    const uint64_t mm = (uint32_t)m;                  // m >= 0: zero-extended
     const uint64_t ph = cc.p_fix * (mm * mm) - qf * mm - cc.d_fix;
     const int64_t sph = (int64_t)ph;
     *sgn = (sph > 0) - (sph < 0);
@@ -908,26 +935,28 @@ __global__ void __launch_bounds__(256) pd_finalize_kernel(
 #pragma unroll
         for (int j = 0; j < 6; ++j) S[j] += (double)p[j * Kc];
     }
+    // FP64 division is slow on this part: one reciprocal per factor, w in {1, 2} by constants
     const int n = pds[pd].n;
     const double NN = (double)N * N;
+    const double inv_n = 1.0 / n, inv_nnn = 1.0 / (NN * n);
     float2* av = avg_spec + (int64_t)pd * 2 * Kc;
     if (mode & 1) {
         // Wiener average (reference :353-366): sum_i F_i C_i / -(sum C^2 + 1/5), / N^2, / n
-        const double wd = -(S[0] + 0.2);
-        av[k] = make_float2((float)(S[1] / wd / NN / n), (float)(S[2] / wd / NN / n));
+        const double q = inv_nnn / -(S[0] + 0.2);
+        av[k] = make_float2((float)(S[1] * q), (float)(S[2] * q));
     }
     if (!(mode & 2)) return;
     const int kb = (int)k % Nh;
-    const double w = (kb == 0 || (N % 2 == 0 && kb == N / 2)) ? 1.0 : 2.0;
-    const double sw = sqrt(w), s2w = sqrt(2.0 * w);
-    const float mu_u = (float)(sw * S[5] / n);
-    float mu_v = (float)(sw * S[0] / n);
+    const bool w1 = kb == 0 || (N % 2 == 0 && kb == N / 2);
+    const double sw = w1 ? 1.0 : 1.4142135623730951, s2w = w1 ? 1.4142135623730951 : 2.0;
+    const float mu_u = (float)(sw * S[5] * inv_n);
+    float mu_v = (float)(sw * S[0] * inv_n);
     if (ring_of) {
-        const float mt = (float)(S[0] / n);
+        const float mt = (float)(S[0] * inv_n);
         mu_v = (float)sw * mt;
         mu[4 * Kc_pad + ring_of[k]] = mt;
     }
-    const float mu_r = (float)(s2w * S[1] / n), mu_s = (float)(s2w * S[2] / n);
+    const float mu_r = (float)(s2w * S[1] * inv_n), mu_s = (float)(s2w * S[2] * inv_n);
     mu[k] = mu_u;
     mu[Kc_pad + k] = mu_v;
     mu[2 * Kc_pad + k] = mu_r;
@@ -935,7 +964,7 @@ __global__ void __launch_bounds__(256) pd_finalize_kernel(
     const float mx = fmaxf(fmaxf(fabsf(mu_u), fabsf(mu_v)), fmaxf(fabsf(mu_r), fabsf(mu_s)));
     atomicMax(pd_max + pd, __float_as_uint(mx));
     // phase-flipped average (:346-348, :367): sum_i sign(C_i) F_i / N^2 / n
-    av[Kc + k] = make_float2((float)(S[3] / NN / n), (float)(S[4] / NN / n));
+    av[Kc + k] = make_float2((float)(S[3] * inv_nnn), (float)(S[4] * inv_nnn));
 }
 
 // ------------------------------------------------------------------------------------------
