@@ -422,6 +422,7 @@ int mem_plan_create(const mem_params* params, int32_t n_pd, const int32_t* pd_co
     L.img_row = take(sizeof(int32_t) * P->n_images);
     L.tiles = take(sizeof(Tile) * P->tiles.size());
     L.qfix = take(sizeof(uint64_t) * P->n_images);
+    L.rotc = take(64 * (size_t)P->n_images);            // two fixed-point rotations per image
     L.gtab = take(sizeof(float) * P->N * P->Nh);
     L.pd_max = take(sizeof(uint32_t) * n_pd);
     L.colmap = take(sizeof(int32_t) * P->ftab.size());
@@ -644,7 +645,7 @@ int execute_impl(mem_plan* plan, const mem_inputs* in, const mem_outputs* out, v
     MEM_STEP(mark(2));
     // (a4, a6) mask and the two rotations -> imgAll
     float* img_all = out->img_all ? out->img_all : xbuf;
-    MEM_STEP(kern::rotate(P, *in, xbuf, img_all, pds, img_pd, spec, s));
+    MEM_STEP(kern::rotate(P, *in, xbuf, img_all, pds, img_pd, spec, at<char>(ws, L.rotc), s));
     MEM_STEP(mark(3));
     // (a8) F = fft2(imgAll); (a7, a9) CTF and per-PD sums.  With a volume mask the spectra of
     // D, of the phase flips and of imgAvgFlip are those of imgAll * msk2 (:344), while the Wiener

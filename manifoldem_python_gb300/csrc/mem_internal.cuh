@@ -76,7 +76,7 @@ struct FeatTables {
 
 struct Layout {
     size_t status, pd_table, sum_items, img_pd, img_row, tiles;
-    size_t item_off, qfix, gtab, pd_max, colmap, twid, ident;
+    size_t item_off, qfix, rotc, gtab, pd_max, colmap, twid, ident;
     size_t xbuf, spec, feat_a, feat_b, pair_norm, partial, means, avg_spec, avg_real, cufft_work;
     size_t total;
 };
@@ -165,8 +165,10 @@ int spectrum_fft(const mem_plan& P, int64_t count, const float* images, const fl
 // signed = the phase-flip inverse: element k of image i multiplied by sign(C_i(k)) / N^2 on load
 int inverse_fft(const mem_plan& P, int64_t count, const float2* spec, const float2* twid,
                 float* images, const uint64_t* qf, bool signed_flip, cudaStream_t s);
+// rot_scratch: 64 bytes per image (the two rotations' fixed-point constants)
 int rotate(const mem_plan& P, const mem_inputs& in, float* xbuf, float* img_out,
-           const PdDev* pd_table, const int32_t* img_pd, float2* spec, cudaStream_t s);
+           const PdDev* pd_table, const int32_t* img_pd, float2* spec, void* rot_scratch,
+           cudaStream_t s);
 int qfix(const mem_plan& P, const mem_inputs& in, uint64_t* qf, cudaStream_t s);
 // which: 1 = S0..S2, 2 = S3..S5, 3 = all six per-PD sums
 int pd_sums(const mem_plan& P, const float2* spec, const uint64_t* qf, const SumItem* items,

@@ -336,6 +336,22 @@ __device__ __forceinline__ RotConst make_rot(double cs, double sn, int N) {
     return R;
 }
 
+// The two rotations of every image: rotatefill by -(180/pi) Psi_i degrees (back to radians),
+// then by the PD's -psi_p (its cosine and sine are in the PD table).  Computed once per image so
+// that the rotation kernels read them instead of one thread per CTA evaluating FP64
+// trigonometry while the CTA waits (FP64 is slow on this part).
+__global__ void rot_const_kernel(const double* __restrict__ psi_rad, const PdDev* __restrict__ pds,
+                                 const int32_t* __restrict__ img_pd, RotConst* __restrict__ out,
+                                 int64_t n, int N) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double ang = -(180.0 / 3.141592653589793) * psi_rad[i];
+    const double t = ang * (3.141592653589793 / 180.0);
+    out[2 * i] = make_rot(cos(t), sin(t), N);
+    const PdDev& pd = pds[img_pd[i]];
+    out[2 * i + 1] = make_rot(pd.rot2_cos, pd.rot2_sin, N);
+}
+
 // one axis of the periodic prefilter over an N x N image in smem (row stride P).
 // axis 0: filter along each row (elements s[r*P + k]); axis 1: along each column.
 template <int NT>
@@ -457,9 +473,8 @@ __device__ __forceinline__ float sample_at(const float* s, int N, int P, int64_t
 // sample coordinates advance by a constant fixed-point step.
 template <int NT, int MAXV>
 __global__ void __launch_bounds__(NT) rotate_kernel(
-        float* __restrict__ xbuf, float* __restrict__ img_out, const double* __restrict__ psi_rad,
-        const PdDev* __restrict__ pds, const int32_t* __restrict__ img_pd, int N, int P,
-        int nseg, float inv1mzN, int exact_init) {
+        float* __restrict__ xbuf, float* __restrict__ img_out, const RotConst* __restrict__ rotc,
+        int N, int P, int nseg, float inv1mzN, int exact_init) {
     extern __shared__ float s[];
     __shared__ RotConst rot[2];
     const int64_t img = blockIdx.x;
@@ -469,14 +484,7 @@ __global__ void __launch_bounds__(NT) rotate_kernel(
     const int c = threadIdx.x % N;
     const int r0 = threadIdx.x / N;
     const bool active = r0 < R;
-    if (threadIdx.x == 0) {
-        // first rotation: rotatefill(img, -(180/pi) Psi) -> t = deg2rad(that)
-        const double ang = -(180.0 / 3.141592653589793) * psi_rad[img];
-        const double t = ang * (3.141592653589793 / 180.0);
-        rot[0] = make_rot(cos(t), sin(t), N);
-        const PdDev& pd = pds[img_pd[img]];
-        rot[1] = make_rot(pd.rot2_cos, pd.rot2_sin, N);
-    }
+    if (threadIdx.x < 2) rot[threadIdx.x] = rotc[2 * img + threadIdx.x];
     // load (storage orientation) into smem in reference orientation, times the mask
     for (int p = threadIdx.x; p < NN; p += NT) {
         const int a = p / N, b = p - a * N;
@@ -690,21 +698,14 @@ __device__ __forceinline__ void rotate_once(const float* s, const RotConst& Q, f
 
 template <int NT, int N>
 __global__ void __launch_bounds__(NT, 2) rotate_fixed_kernel(
-        float* __restrict__ xbuf, float* __restrict__ img_out, const double* __restrict__ psi_rad,
-        const PdDev* __restrict__ pds, const int32_t* __restrict__ img_pd) {
+        float* __restrict__ xbuf, float* __restrict__ img_out, const RotConst* __restrict__ rotc) {
     constexpr int P = rot_stride<N>(), NN = N * N, R = NT / N, MAXV = N / R;
     extern __shared__ float s[];
     __shared__ RotConst rot[2];
     __shared__ float carry[2 * rot_nseg<NT, N>() * N];
     const int64_t img = blockIdx.x;
     float* xi = xbuf + img * (int64_t)NN;
-    if (threadIdx.x == 0) {
-        const double ang = -(180.0 / 3.141592653589793) * psi_rad[img];
-        const double t = ang * (3.141592653589793 / 180.0);
-        rot[0] = make_rot(cos(t), sin(t), N);
-        const PdDev& pd = pds[img_pd[img]];
-        rot[1] = make_rot(pd.rot2_cos, pd.rot2_sin, N);
-    }
+    if (threadIdx.x < 2) rot[threadIdx.x] = rotc[2 * img + threadIdx.x];
     for (int p = threadIdx.x; p < NN; p += NT) {
         const int a = p / N, b = p % N;
         s[b * P + a] = xi[p] * mask_ref(b, a, N);
@@ -755,20 +756,13 @@ __device__ __forceinline__ float sample_wrap(const float* s, int N, int64_t X, i
 template <int NT>
 __global__ void __launch_bounds__(NT) rotate_global_kernel(
         float* __restrict__ xbuf, float2* __restrict__ spec, int64_t Kc, float* __restrict__ img_out,
-        const double* __restrict__ psi_rad, const PdDev* __restrict__ pds,
-        const int32_t* __restrict__ img_pd, int N, int nseg, float inv1mzN) {
+        const RotConst* __restrict__ rotc, int N, int nseg, float inv1mzN) {
     __shared__ RotConst rot[2];
     const int64_t img = blockIdx.x;
     const int NN = N * N;
     float* B = xbuf + img * (int64_t)NN;
     float* A = reinterpret_cast<float*>(spec + img * Kc);
-    if (threadIdx.x == 0) {
-        const double ang = -(180.0 / 3.141592653589793) * psi_rad[img];
-        const double t = ang * (3.141592653589793 / 180.0);
-        rot[0] = make_rot(cos(t), sin(t), N);
-        const PdDev& pd = pds[img_pd[img]];
-        rot[1] = make_rot(pd.rot2_cos, pd.rot2_sin, N);
-    }
+    if (threadIdx.x < 2) rot[threadIdx.x] = rotc[2 * img + threadIdx.x];
     for (int p = threadIdx.x; p < NN; p += NT) {          // masked, back to reference orientation
         const int r = p / N, c = p - r * N;
         A[p] = B[c * N + r] * mask_ref(r, c, N);
@@ -1244,14 +1238,19 @@ int lowpass_table(const mem_plan& P, float* gtab, cudaStream_t s) {
 }
 
 int rotate(const mem_plan& P, const mem_inputs& in, float* xbuf, float* img_out,
-           const PdDev* pd_table, const int32_t* img_pd, float2* spec, cudaStream_t s) {
+           const PdDev* pd_table, const int32_t* img_pd, float2* spec, void* rot_scratch,
+           cudaStream_t s) {
     if (P.n_images == 0) return MEM_OK;
     const int N = P.N;
+    RotConst* rotc = static_cast<RotConst*>(rot_scratch);
+    rot_const_kernel<<<(unsigned)((P.n_images + 255) / 256), 256, 0, s>>>(
+        in.psi_rad, pd_table, img_pd, rotc, P.n_images, N);
+    MEM_LAUNCH_CHECK();
     if (N > kMaxSmemN) {
         constexpr int NT = 512;
         const int nseg = std::max(1, std::min(NT / N, N / 16));
         rotate_global_kernel<NT><<<(unsigned)P.n_images, NT, 0, s>>>(
-            xbuf, spec, P.Kc, img_out, in.psi_rad, pd_table, img_pd, N, nseg,
+            xbuf, spec, P.Kc, img_out, rotc, N, nseg,
             (float)(1.0 / (1.0 - std::pow((double)kZ1, (double)N))));
         MEM_LAUNCH_CHECK();
         return MEM_OK;
@@ -1265,7 +1264,7 @@ int rotate(const mem_plan& P, const mem_inputs& in, float* xbuf, float* img_out,
                               (N == 128 ? rot_stride<128>() : rot_stride<64>()) * sizeof(float);
         MEM_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)smem_f));
-        kfn<<<(unsigned)P.n_images, NT, smem_f, s>>>(xbuf, img_out, in.psi_rad, pd_table, img_pd);
+        kfn<<<(unsigned)P.n_images, NT, smem_f, s>>>(xbuf, img_out, rotc);
         MEM_LAUNCH_CHECK();
         return MEM_OK;
     }
@@ -1279,12 +1278,12 @@ int rotate(const mem_plan& P, const mem_inputs& in, float* xbuf, float* img_out,
         MEM_CUDA_TRY(cudaFuncSetAttribute(rotate_kernel<NT, 32>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         rotate_kernel<NT, 32><<<(unsigned)P.n_images, NT, smem, s>>>(
-            xbuf, img_out, in.psi_rad, pd_table, img_pd, N, Pst, nseg, inv1mzN, exact ? 1 : 0);
+            xbuf, img_out, rotc, N, Pst, nseg, inv1mzN, exact ? 1 : 0);
     } else {
         MEM_CUDA_TRY(cudaFuncSetAttribute(rotate_kernel<NT, 0>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         rotate_kernel<NT, 0><<<(unsigned)P.n_images, NT, smem, s>>>(
-            xbuf, img_out, in.psi_rad, pd_table, img_pd, N, Pst, nseg, inv1mzN, exact ? 1 : 0);
+            xbuf, img_out, rotc, N, Pst, nseg, inv1mzN, exact ? 1 : 0);
     }
     MEM_LAUNCH_CHECK();
     return MEM_OK;

@@ -210,7 +210,8 @@ def workspace_bytes_per_image(params: StageParams) -> int:
     """Approximate device bytes one image needs (workspace and full outputs)."""
     N = params.N
     feat = 4 * feature_columns(N)          # FP32 features, or bf16 hi + lo
-    return 4 * N * N * 4 + 8 * N * (N // 2 + 1) + feat + 64
+    # + per-image tables: defocus phase, PD / row indices, pair norm, two rotations (64 B)
+    return 4 * N * N * 4 + 8 * N * (N // 2 + 1) + feat + 128
 
 
 def admit_batches(counts: Sequence[int], params: StageParams, budget_bytes: int) -> List[List[int]]:
