@@ -689,10 +689,10 @@ def main():
                     help='streamed: stack left in pinned host memory, PD groups pipelined over '
                          'load / compute / copy streams; copy: one host-to-device copy of the '
                          'stack, then one execute')
-    ap.add_argument('--e2e-groups', type=int, default=10)
-    ap.add_argument('--e2e-ramp', type=float, default=1.5,
+    ap.add_argument('--e2e-groups', type=int, default=11)
+    ap.add_argument('--e2e-ramp', type=float, default=1.35,
                     help='growth factor of the first PD groups of the streamed e2e pass')
-    ap.add_argument('--e2e-ramp-steps', type=int, default=4)
+    ap.add_argument('--e2e-ramp-steps', type=int, default=5)
     ap.add_argument('--no-dm', action='store_true',
                     help='skip the diffusion-map embedding of a sample of PDs (GPU vs CPU port)')
     ap.add_argument('--dm-pds', type=int, default=8)

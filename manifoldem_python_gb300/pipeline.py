@@ -362,10 +362,11 @@ class StreamedStage:
     """The stage for many PDs with the image stack left in pinned host memory.
 
     The PDs are split into ``n_groups`` consecutive groups, one plan each, of about equal image
-    count after a geometric ramp over the first ``ramp_steps`` groups (``balanced_groups``): the
-    host link delivers images about 1.5x faster than the stage computes them, so each group may
-    be up to that much larger than the one before without the compute stream waiting, and a
-    small first group shortens the wait before the first computation.  Every ``run`` issues, per group, the per-image metadata copy and the stack-reading
+    count after a geometric ramp over the first ``ramp_steps`` groups (``balanced_groups``): at
+    128 px the host link delivers images about 1.3x faster than the stage computes them (0.31 us
+    against 0.41 us per image on a GB300), so each group may be up to about that much larger than
+    the one before without the compute stream waiting, and a small first group shortens the wait
+    before the first computation.  Every ``run`` issues, per group, the per-image metadata copy and the stack-reading
     kernel on a high-priority load stream (a small grid reading the images over the host link,
     ``mem_plan_execute_split``), the rest of the stage on a compute stream, and the copy of the
     results into pinned host buffers on a copy stream.  Group g+1's images arrive while group g
@@ -373,8 +374,8 @@ class StreamedStage:
     """
 
     def __init__(self, params: StageParams, counts: Sequence[int], psi_p: Sequence[float],
-                 n_groups: int = 10, outputs=('D', 'img_avg', 'img_avg_flip', 'img_all_intensity'),
-                 device=None, ramp: float = 1.5, ramp_steps: int = 4):
+                 n_groups: int = 11, outputs=('D', 'img_avg', 'img_avg_flip', 'img_all_intensity'),
+                 device=None, ramp: float = 1.35, ramp_steps: int = 5):
         import torch
         self.device = torch.device(device or 'cuda')
         self.counts = [int(c) for c in counts]
