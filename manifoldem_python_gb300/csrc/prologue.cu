@@ -317,9 +317,11 @@ __global__ void lowpass_apply_kernel(float2* __restrict__ spec, const float* __r
 //   out[r][c] = sum_{i,j} coef[x_i][y_j] B3(x - x_i) B3(y - y_j),
 //   x = cos t (r-c0) + sin t (c-c0) + c0,  y = -sin t (r-c0) + cos t (c-c0) + c0.
 // coef is the periodic prefilter of the image: the causal/anticausal recursion with pole
-// z1 = sqrt(3) - 2, each row (then column) split into segments whose start values are the
-// truncated geometric sums over the previous kInitTaps samples (exact to |z1|^24).
-// Sample coordinates are computed in 64-bit fixed point (32 fractional bits).
+// z1 = sqrt(3) - 2, each row (then column) split into segments.  The runtime-size kernels start
+// each segment from the truncated geometric sum over the previous kInitTaps samples (exact to
+// |z1|^18); the compile-time kernels hold the segments in registers and start them from their
+// neighbours' end states (prefilter_fixed).  Sample coordinates are computed in 64-bit fixed
+// point (32 fractional bits) from constants made once per image (rot_const_kernel).
 // ------------------------------------------------------------------------------------------
 struct RotConst {
     int64_t bx, by, rc, rs;   // fixed-point x = bx + r rc + c rs, y = by - r rs + c rc
