@@ -462,7 +462,7 @@ __device__ __forceinline__ void lowpass_image(
     const float* src = stack + s * (int64_t)NN;
     // rows (2p, 2p+1) -> Z_p at natural positions; background statistics (:277-281)
     KSumF sum, sq;
-#pragma unroll 1
+#pragma unroll 2
     for (int i = 0; i < F::IT1; ++i) {
         const int p = 8 * w + F::LP1 * i + l / R2, t = l % R2;
 #pragma unroll
