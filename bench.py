@@ -386,12 +386,13 @@ def workload_string(config_name, cfg, counts):
 
 def kernels_per_execute(outputs, avg_only, N):
     """Kernels of this library one mem_plan_execute launches (cuFFT kernels excluded).
-    N = 32, 64, 128 (shared-memory FFTs): lowpass_table, lowpass_fft, rotate, spectrum_fft,
-    qfix, pd_sums, pd_finalize, features, [inverse_fft + avg_store], [inverse_fft + intensity],
-    [contraction].  Other N (cuFFT transforms): lowpass_table, gather_normalize, lowpass_apply,
-    rotate, qfix, pd_sums, pd_finalize, features, [avg_store], [intensity], [contraction]."""
+    N = 32, 64, 128 (shared-memory FFTs): lowpass_table, lowpass_fft, rot_const, rotate,
+    spectrum_fft, qfix, pd_sums, pd_finalize, features, [inverse_fft + avg_store],
+    [inverse_fft + intensity], [contraction].  Other N (cuFFT transforms): lowpass_table,
+    gather_normalize, lowpass_apply, rot_const, rotate, qfix, pd_sums, pd_finalize, features,
+    [avg_store], [intensity], [contraction]."""
     smem = N in (32, 64, 128) and os.environ.get('MEM_SMEM_FFT', '1') != '0'
-    k = 8
+    k = 9
     if 'img_avg' in outputs or 'img_avg_flip' in outputs:
         k += 2 if smem else 1
     if smem and ('img_all_intensity' in outputs or 'img_all_flip' in outputs):
