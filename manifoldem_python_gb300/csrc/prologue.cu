@@ -721,6 +721,15 @@ __global__ void __launch_bounds__(NT, 2) rotate_fixed_kernel(
         float keep[MAXV];
         int base, stride;
         rotate_once<NT, N>(s, rot[pass], keep, base, stride);
+        if (pass == 1 && stride == R * P) {
+            // lanes along output rows (the same for the whole CTA): keep[k] is output
+            // (t / N + k R, t % N), so the stores are coalesced without staging
+            float* out = img_out + img * (int64_t)NN;
+            const int u = threadIdx.x % N, v0 = threadIdx.x / N;
+#pragma unroll
+            for (int k = 0; k < MAXV; ++k) out[(v0 + k * R) * N + u] = keep[k];
+            return;
+        }
         __syncthreads();
 #pragma unroll
         for (int k = 0; k < MAXV; ++k) s[base + k * stride] = keep[k];
