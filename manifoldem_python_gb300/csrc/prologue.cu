@@ -571,9 +571,11 @@ __device__ constexpr float z1_pow() {
 // the CT = ceil(32 / SEG) previous segments (the rest of the periodic sum is below
 // z1^32 = 5e-19 of it); the recursion then runs from that state.  The anticausal pass c-[k] = c+[k] + z1 c-[k+1] does the
 // same from the segment's end, and the output is -6 z1 c-[k].  Each sample is read and written
-// once; segment states go through carry[] (2 NSEG N floats).
-template <int NT, int N, int AXIS>
-__device__ __forceinline__ void prefilter_fixed(float* s, float* carry) {
+// once; segment states go through carry[] (2 NSEG N floats).  FROM_REGS: the thread's segment
+// is taken from vin[] (a rotation's samples, see rotate_once) instead of shared memory.
+template <int NT, int N, int AXIS, bool FROM_REGS = false>
+__device__ __forceinline__ void prefilter_fixed(float* s, float* carry,
+                                                const float* vin = nullptr) {
     constexpr int P = rot_stride<N>();
     constexpr int NSEG = rot_nseg<NT, N>();
     constexpr int SEG = N / NSEG, LINES = N * NSEG;
@@ -593,7 +595,7 @@ __device__ __forceinline__ void prefilter_fixed(float* s, float* carry) {
         float e = 0.f;
 #pragma unroll
         for (int k = 0; k < SEG; ++k) {
-            v[k] = b0[k * SK];
+            v[k] = FROM_REGS ? vin[k] : b0[k * SK];
             e = fmaf(kZ1, e, v[k]);
         }
         carry_c[g * N + line] = e;
@@ -670,22 +672,22 @@ __device__ __forceinline__ float2 sample_fixed2(const float* s, int64_t XA, int6
 }
 
 // One rotation of the coefficient image in smem into keep[]: thread t has u = t % N and
-// v0 = t / N; it samples output (r, c) = (v0 + k R, u) when the lanes run along output rows
-// (lane step (sin, cos) in (x, y)), or (u, v0 + k R) when they run along output columns (lane
-// step (cos, -sin)) -- whichever step has components of one sign.  Returns the smem index of
-// keep[0] and the stride of keep[k] in the [r][c] layout.
+// g = t / N; it samples the MAXV outputs (r, c) = (g MAXV + k, u) when the lanes run along
+// output rows (lane step (sin, cos) in (x, y)), or (u, g MAXV + k) when they run along output
+// columns (lane step (cos, -sin)) -- whichever step has components of one sign.  keep[] is then
+// segment g of column u (rows) or of row u (columns): the segment prefilter_fixed gives thread t
+// along axis 1 or 0.  Returns whether the lanes run along columns.
 template <int NT, int N>
-__device__ __forceinline__ void rotate_once(const float* s, const RotConst& Q, float* keep,
-                                            int& base, int& stride) {
-    constexpr int P = rot_stride<N>(), R = NT / N, MAXV = N / R;
+__device__ __forceinline__ bool rotate_once(const float* s, const RotConst& Q, float* keep) {
+    constexpr int R = NT / N, MAXV = N / R;
     constexpr int64_t kOne = 1ll << 32;
-    const int u = threadIdx.x % N, v0 = threadIdx.x / N;
+    const int u = threadIdx.x % N, v0 = (threadIdx.x / N) * MAXV;
     const bool along_cols = (Q.rc > 0) != (Q.rs > 0);
     const int r = along_cols ? u : v0, c = along_cols ? v0 : u;
     int64_t X = Q.bx - kOne + (int64_t)r * Q.rc + (int64_t)c * Q.rs;
     int64_t Y = Q.by - kOne - (int64_t)r * Q.rs + (int64_t)c * Q.rc;
-    const int64_t dX = (int64_t)R * (along_cols ? Q.rs : Q.rc);
-    const int64_t dY = (int64_t)R * (along_cols ? Q.rc : -Q.rs);
+    const int64_t dX = along_cols ? Q.rs : Q.rc;
+    const int64_t dY = along_cols ? Q.rc : -Q.rs;
 #pragma unroll
     for (int k = 0; k < MAXV; k += 2) {
         const float2 v = sample_fixed2<N>(s, X, Y, X + dX, Y + dY);
@@ -694,8 +696,7 @@ __device__ __forceinline__ void rotate_once(const float* s, const RotConst& Q, f
         X += 2 * dX;
         Y += 2 * dY;
     }
-    base = r * P + c;
-    stride = along_cols ? R : R * P;
+    return along_cols;
 }
 
 template <int NT, int N>
@@ -713,29 +714,34 @@ __global__ void __launch_bounds__(NT, 2) rotate_fixed_kernel(
         s[b * P + a] = xi[p] * mask_ref(b, a, N);
     }
     __syncthreads();
-#pragma unroll 1
-    for (int pass = 0; pass < 2; ++pass) {
-        prefilter_fixed<NT, N, 0>(s, carry);
+    static_assert(MAXV == N / rot_nseg<NT, N>(), "a rotation's samples are one prefilter segment");
+    prefilter_fixed<NT, N, 0>(s, carry);
+    prefilter_fixed<NT, N, 1>(s, carry);
+    fill_halo<NT>(s, N, P);
+    float keep[MAXV];
+    // the second prefilter starts on the axis of the first rotation's samples, from registers
+    // (the prefilter's barriers precede its stores, so every thread has finished sampling)
+    if (rotate_once<NT, N>(s, rot[0], keep)) {
+        prefilter_fixed<NT, N, 0, true>(s, carry, keep);
         prefilter_fixed<NT, N, 1>(s, carry);
-        fill_halo<NT>(s, N, P);
-        float keep[MAXV];
-        int base, stride;
-        rotate_once<NT, N>(s, rot[pass], keep, base, stride);
-        if (pass == 1 && stride == R * P) {
-            // lanes along output rows (the same for the whole CTA): keep[k] is output
-            // (t / N + k R, t % N), so the stores are coalesced without staging
-            float* out = img_out + img * (int64_t)NN;
-            const int u = threadIdx.x % N, v0 = threadIdx.x / N;
-#pragma unroll
-            for (int k = 0; k < MAXV; ++k) out[(v0 + k * R) * N + u] = keep[k];
-            return;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int k = 0; k < MAXV; ++k) s[base + k * stride] = keep[k];
-        __syncthreads();
+    } else {
+        prefilter_fixed<NT, N, 1, true>(s, carry, keep);
+        prefilter_fixed<NT, N, 0>(s, carry);
     }
+    fill_halo<NT>(s, N, P);
+    const bool along_cols = rotate_once<NT, N>(s, rot[1], keep);
     float* out = img_out + img * (int64_t)NN;
+    const int u = threadIdx.x % N, v0 = (threadIdx.x / N) * MAXV;
+    if (!along_cols) {
+        // keep[k] is output (v0 + k, u): coalesced stores without staging
+#pragma unroll
+        for (int k = 0; k < MAXV; ++k) out[(v0 + k) * N + u] = keep[k];
+        return;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < MAXV; ++k) s[u * P + v0 + k] = keep[k];     // output (u, v0 + k)
+    __syncthreads();
     for (int p = threadIdx.x; p < NN; p += NT) out[p] = s[(p / N) * P + p % N];
 }
 
