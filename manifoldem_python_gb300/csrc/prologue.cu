@@ -709,16 +709,20 @@ __global__ void __launch_bounds__(NT, 2) rotate_fixed_kernel(
     const int64_t img = blockIdx.x;
     float* xi = xbuf + img * (int64_t)NN;
     if (threadIdx.x < 2) rot[threadIdx.x] = rotc[2 * img + threadIdx.x];
-    for (int p = threadIdx.x; p < NN; p += NT) {
-        const int a = p / N, b = p % N;
-        s[b * P + a] = xi[p] * mask_ref(b, a, N);
-    }
-    __syncthreads();
     static_assert(MAXV == N / rot_nseg<NT, N>(), "a rotation's samples are one prefilter segment");
-    prefilter_fixed<NT, N, 0>(s, carry);
+    float keep[MAXV];
+    {
+        // the masked image (stored transposed: s row b = image column b), thread t's first
+        // prefilter segment read straight from global memory: image column t % N, rows
+        // (t / N) MAXV .. + MAXV - 1 (lanes on consecutive columns: coalesced)
+        const int line = threadIdx.x % N, a0 = (threadIdx.x / N) * MAXV;
+#pragma unroll
+        for (int k = 0; k < MAXV; ++k)
+            keep[k] = xi[(a0 + k) * N + line] * mask_ref(line, a0 + k, N);
+    }
+    prefilter_fixed<NT, N, 0, true>(s, carry, keep);
     prefilter_fixed<NT, N, 1>(s, carry);
     fill_halo<NT>(s, N, P);
-    float keep[MAXV];
     // the second prefilter starts on the axis of the first rotation's samples, from registers
     // (the prefilter's barriers precede its stores, so every thread has finished sampling)
     if (rotate_once<NT, N>(s, rot[0], keep)) {
