@@ -413,39 +413,14 @@ def traffic_from_profiles(kernel_tag, workload):
     return float(m.group(1)) if m else None
 
 
-def run_gpu(args, rank, world):
+def time_form(plan, stack, sidx, flip, psi, dfd, outs, args, world, dev, flush):
+    """Device time of one step of ``plan`` (CUDA graph replay unless --no-graph): W untimed
+    warm-up steps, then exactly K steps timed with CUDA events on the launching stream between
+    a barrier and a synchronize; when the stack is smaller than twice L2 every step is timed
+    alone after a write of a buffer larger than L2.  Returns (ms per step, max over ranks;
+    per-phase ms of one extra step timed by the library's phase events; the graph)."""
+    import ctypes
     import torch
-    from manifoldem_python_gb300.pipeline import Plan, StageParams
-    from manifoldem_python_gb300.geometry import pd_geometry
-    from manifoldem_python_gb300.synthetic import CONFIGS, make_dataset
-    import dataclasses
-
-    dev = torch.device('cuda', int(os.environ.get('LOCAL_RANK', 0)))
-    torch.cuda.set_device(dev)
-    cfg = CONFIGS[args.config]
-    if args.n_pd:
-        cfg = dataclasses.replace(cfg, n_pd=args.n_pd)
-    cfg = dataclasses.replace(cfg, seed=cfg.seed + 1000 * rank)
-    t0 = time.time()
-    ds = make_dataset(cfg, device=dev)
-    torch.cuda.synchronize(dev)
-    t_gen = time.time() - t0
-    geoms = [pd_geometry(np.asarray(ind), ds.q[:, ind], ds.nStot) for ind in ds.CG]
-    counts = [int(len(ind)) for ind in ds.CG]
-    params = StageParams(N=cfg.N, pix_size=cfg.pix, Cs=cfg.cs, EkV=cfg.kv,
-                         AmpContrast=cfg.ampc, precision=args.precision)
-    plan = Plan(params, counts, [g.psi_p for g in geoms], dev)
-    outputs = tuple(args.outputs.split(','))
-    outs = plan.allocate_outputs(outputs)
-    sidx_h = np.concatenate([g.stack_index for g in geoms])
-    flip_h = np.concatenate([g.flip for g in geoms])
-    psi_h = np.concatenate([g.psi_rad for g in geoms])
-    df_h = np.concatenate([ds.df[ind] for ind in ds.CG]).astype(np.float64)
-    sidx = torch.from_numpy(sidx_h).to(dev)
-    flip = torch.from_numpy(flip_h).to(dev)
-    psi = torch.from_numpy(psi_h).to(dev)
-    dfd = torch.from_numpy(df_h).to(dev)
-    stack = ds.stack
     stream = torch.cuda.current_stream(dev)
     graph = None
     if args.graph:
@@ -468,25 +443,21 @@ def run_gpu(args, rank, world):
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize(dev)
-    # an image stack smaller than twice L2 could stay cached between steps: then every step is
-    # timed alone, after a write of a buffer larger than L2 outside its event pair
-    flush = stack.numel() * stack.element_size() < 2 * L2_BYTES
     scrub = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev) if flush else None
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(args.steps if flush else 1)]
-    with ClockSampler(dev.index) as clk:
-        if flush:
-            for e0, e1 in ev:
-                scrub.fill_(1.0)
-                e0.record(stream)
-                step()
-                e1.record(stream)
-        else:
-            ev[0][0].record(stream)
-            for _ in range(args.steps):
-                step()
-            ev[0][1].record(stream)
-        torch.cuda.synchronize(dev)
+    if flush:
+        for e0, e1 in ev:
+            scrub.fill_(1.0)
+            e0.record(stream)
+            step()
+            e1.record(stream)
+    else:
+        ev[0][0].record(stream)
+        for _ in range(args.steps):
+            step()
+        ev[0][1].record(stream)
+    torch.cuda.synchronize(dev)
     ms = sum(e0.elapsed_time(e1) for e0, e1 in ev) / args.steps
     del scrub
     if world > 1:
@@ -494,9 +465,7 @@ def run_gpu(args, rank, world):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
     plan.device_status()
-
-    # live phase timing of one step (CUDA events between the phases)
-    import ctypes
+    # live phase timing of one more step (CUDA events between the phases)
     lib = plan.lib
     lib.mem_plan_set_timing(plan.handle, 1)
     plan.execute(stack, sidx, flip, psi, dfd, outs, stream)
@@ -504,6 +473,76 @@ def run_gpu(args, rank, world):
     lib.mem_plan_phase_times(plan.handle, phase_ms, 9)
     lib.mem_plan_set_timing(plan.handle, 0)
     phases = {lib.mem_phase_name(i).decode(): float(phase_ms[i]) for i in range(9)}
+    return ms, phases, graph
+
+
+def run_gpu(args, rank, world):
+    import torch
+    from manifoldem_python_gb300.pipeline import Plan, StageParams
+    from manifoldem_python_gb300.geometry import pd_geometry
+    from manifoldem_python_gb300.synthetic import CONFIGS, make_dataset
+    import dataclasses
+
+    dev = torch.device('cuda', int(os.environ.get('LOCAL_RANK', 0)))
+    torch.cuda.set_device(dev)
+    cfg = CONFIGS[args.config]
+    if args.n_pd:
+        cfg = dataclasses.replace(cfg, n_pd=args.n_pd)
+    cfg = dataclasses.replace(cfg, seed=cfg.seed + 1000 * rank)
+    t0 = time.time()
+    ds = make_dataset(cfg, device=dev)
+    torch.cuda.synchronize(dev)
+    t_gen = time.time() - t0
+    geoms = [pd_geometry(np.asarray(ind), ds.q[:, ind], ds.nStot) for ind in ds.CG]
+    counts = [int(len(ind)) for ind in ds.CG]
+    params = StageParams(N=cfg.N, pix_size=cfg.pix, Cs=cfg.cs, EkV=cfg.kv,
+                         AmpContrast=cfg.ampc, precision=args.precision)
+    # the contraction schedule per PD size class: measured by the autotuner (cached per GPU and
+    # box size), outside the timed region
+    tuned, t_tune = None, 0.0
+    if args.autotune and params.precision == 'bf16x3':
+        from manifoldem_python_gb300 import autotune
+        t0 = time.time()
+        tuned = autotune.tune(params, dev, force=args.autotune == 'force')
+        t_tune = time.time() - t0
+    plan = Plan(params, counts, [g.psi_p for g in geoms], dev)
+    outputs = tuple(args.outputs.split(','))
+    outs = plan.allocate_outputs(outputs)
+    sidx_h = np.concatenate([g.stack_index for g in geoms])
+    flip_h = np.concatenate([g.flip for g in geoms])
+    psi_h = np.concatenate([g.psi_rad for g in geoms])
+    df_h = np.concatenate([ds.df[ind] for ind in ds.CG]).astype(np.float64)
+    sidx = torch.from_numpy(sidx_h).to(dev)
+    flip = torch.from_numpy(flip_h).to(dev)
+    psi = torch.from_numpy(psi_h).to(dev)
+    dfd = torch.from_numpy(df_h).to(dev)
+    stack = ds.stack
+    stream = torch.cuda.current_stream(dev)
+    flush = stack.numel() * stack.element_size() < 2 * L2_BYTES
+    with ClockSampler(dev.index) as clk:
+        ms, phases, graph = time_form(plan, stack, sidx, flip, psi, dfd, outs, args, world, dev,
+                                      flush)
+        graph_used = graph is not None
+        # the other contraction form(s) on the same PDs, images and outputs (the metric compares
+        # split-BF16 with the plain FP32 form): a plan of its own, timed the same way
+        forms = {args.precision: dict(ms_per_step=ms, contraction_ms=phases['contraction'],
+                                      pairs_per_s=plan.n_pairs / (ms * 1e-3), phases_ms=phases)}
+        for other in [f for f in args.forms.split(',') if f and f != args.precision]:
+            oparams = dataclasses.replace(params, precision=other)
+            oplan = Plan(oparams, counts, [g.psi_p for g in geoms], dev)
+            oms, ophases, ograph = time_form(oplan, stack, sidx, flip, psi, dfd, outs, args,
+                                             world, dev, flush)
+            forms[other] = dict(ms_per_step=oms, contraction_ms=ophases['contraction'],
+                                pairs_per_s=oplan.n_pairs / (oms * 1e-3), phases_ms=ophases)
+            del ograph, oplan
+            torch.cuda.synchronize(dev)
+            torch.cuda.empty_cache()
+    del graph
+    if len(forms) > 1:      # the outputs hold the benchmarked form's results again
+        plan.execute(stack, sidx, flip, psi, dfd, outs, stream)
+        torch.cuda.synchronize(dev)
+    if world > 1:
+        torch.distributed.barrier()
 
     dm = None
     if not args.no_dm and 'D' in outs and rank == 0:
@@ -514,7 +553,7 @@ def run_gpu(args, rank, world):
 
     # end to end through the public API with host buffers
     e2e = None
-    n_pairs, n_images, graph_used = plan.n_pairs, plan.n_images, graph is not None
+    n_pairs, n_images = plan.n_pairs, plan.n_images
     if not args.no_e2e:
         pin = True
         try:
@@ -528,7 +567,7 @@ def run_gpu(args, rank, world):
             # the stack stays in pinned host memory; per group of PDs the load kernel reads its
             # images over the host link while the previous group computes (StreamedStage)
             from manifoldem_python_gb300.pipeline import StreamedStage
-            del graph, outs, plan
+            del outs, plan
             ds.stack = stack_h          # later host-side uses read the pinned copy
             del stack
             torch.cuda.empty_cache()
@@ -576,7 +615,7 @@ def run_gpu(args, rank, world):
         e2e = dict(ms=e2e_ms, h2d=int(h2d), d2h=int(d2h), pinned=pin, mode=mode)
         del stack_h
     return dict(ms=ms, pairs=n_pairs, n_images=n_images, counts=counts,
-                graph=graph_used, l2_flush=flush,
+                graph=graph_used, l2_flush=flush, forms=forms, tuned=tuned, t_tune=t_tune,
                 phases=phases, clocks=clk.summary(), t_gen=t_gen, e2e=e2e, ds=ds, cfg=cfg, dm=dm,
                 nlsa=nlsa,
                 kernels=kernels_per_execute(outputs, False, cfg.N), outputs=outputs)
@@ -646,6 +685,79 @@ def precision_report(args, ds, counts, cfg, precision):
                 dm_top8_subspace_angle_rad=top8_subspace_angle(D, ref))
 
 
+def fullsize_precision(ds, cfg, dev, pd=0):
+    """D of one whole PD of the workload (config3: 4000 images of 192 px, 5% near-duplicates) in
+    the split-BF16 form against an FP64 contraction of the GPU's own spectra with exact FP64
+    CTFs, computed on the device in float64: normwise error, the error scaled by each pair's
+    cross-norm term S_ij (the scale below which the GEMM form cancels), the elementwise relative
+    error on the near-duplicate pairs, and the largest principal angle between the top-8
+    diffusion-map coordinates (DMembeddingII.op, k = n, tune 3) of the two matrices."""
+    import torch
+    from scipy.linalg import subspace_angles
+    from manifoldem_python_gb300 import DMembeddingII
+    from manifoldem_python_gb300.pipeline import DistanceStage, PdJob, StageParams
+    ind = np.asarray(ds.CG[pd])
+    n, N = int(ind.size), cfg.N
+    stage = DistanceStage(StageParams(N=N, pix_size=cfg.pix, Cs=cfg.cs, EkV=cfg.kv,
+                                      AmpContrast=cfg.ampc, precision='bf16x3'), device=dev)
+    res = stage.run([PdJob(ind=ind, q=ds.q[:, ind], df=ds.df[ind])], ds.stack, ds.nStot,
+                    outputs=('D', 'spectrum'), to_host=False)[0]
+    f64 = torch.float64
+    F = torch.view_as_complex(res['spectrum'].contiguous()).to(torch.complex128).reshape(n, -1)
+    Nh = N // 2 + 1
+    ka = torch.arange(N, device=dev)
+    fa = torch.minimum(ka, N - ka).to(f64)
+    kb = torch.arange(Nh, device=dev, dtype=f64)
+    k2 = ((fa[:, None] ** 2 + kb[None, :] ** 2) / (N * cfg.pix) ** 2).reshape(-1)
+    lam = 12.3986 / math.sqrt((2 * 511.0 + cfg.kv) * cfg.kv)
+    dfd = torch.as_tensor(np.asarray(ds.df[ind], dtype=np.float64), device=dev)
+    wr = (0.5 * math.pi * cfg.cs * 1e7 * lam ** 3 * k2[None, :] - math.pi * lam * dfd[:, None]) \
+        * k2[None, :]
+    C = torch.sin(wr) - cfg.ampc * torch.cos(wr)                  # ctemh_cryoFrank, no envelope
+    w = torch.full((N, Nh), 2.0, device=dev, dtype=f64)
+    w[:, 0] = 1.0
+    if N % 2 == 0:
+        w[:, -1] = 1.0
+    w = w.reshape(-1)
+    a = (w[None, :] * F.abs() ** 2)                                 # n x Kc
+    A = a @ (C ** 2).T                                              # A[i, j] = sum w |F_i|^2 C_j^2
+    H = torch.sqrt(w)[None, :] * C * F
+    G = (H @ H.conj().T).real
+    S = A + A.T
+    D64 = S - 2 * G
+    D64.fill_diagonal_(0.0)
+    D = res['D']
+    off = ~torch.eye(n, dtype=torch.bool, device=dev)
+    dd = (D - D64).abs()
+    rep = dict(pd=pd, n=n, form='bf16x3',
+               max_rel_err_vs_fp64_contraction=float(dd.max() / D64.abs().max()),
+               max_err_scaled_by_S=float((dd[off] / S[off]).max()))
+    dup = np.asarray(ds.near_dup_of)
+    pos = {int(g): i for i, g in enumerate(np.where(ind >= ds.num_part, ind - ds.num_part, ind))}
+    pairs = [(pos[int(d)], pos[int(s_)]) for d, s_ in enumerate(dup)
+             if s_ >= 0 and int(d) in pos and int(s_) in pos]
+    if pairs:
+        ii = torch.as_tensor([p[0] for p in pairs], device=dev)
+        jj = torch.as_tensor([p[1] for p in pairs], device=dev)
+        rel_el = (D[ii, jj] - D64[ii, jj]).abs() / D64[ii, jj].abs()
+        rep.update(near_duplicate_pairs=len(pairs),
+                   near_duplicate_max_elementwise_rel_err=float(rel_el.max()),
+                   near_duplicate_median_elementwise_rel_err=float(rel_el.median()),
+                   near_duplicate_D_over_S=float((D64[ii, jj] / S[ii, jj]).median()))
+    del A, G, H, S, F, a, C
+    Dh, D64h = D.cpu().numpy(), D64.cpu().numpy()
+    t0 = time.time()
+    np.random.seed(0)
+    pa = DMembeddingII.op(Dh, n, 3, 60000)[1]
+    np.random.seed(0)
+    pb = DMembeddingII.op(D64h, n, 3, 60000)[1]
+    rep['dm_top8_subspace_angle_rad'] = float(np.max(subspace_angles(pa[:, :8], pb[:, :8])))
+    rep['dm_seconds'] = time.time() - t0
+    rep['method'] = ('FP64 D of the GPU spectra and exact CTFs by float64 GEMMs on the device '
+                     '(A + A^T - 2 Re(H H^H)); diffusion maps by the GPU DMembeddingII.op')
+    return rep
+
+
 def cpu_baseline(args, ds, counts, cfg, steps=1, budget_s=20.0):
     cores = os.cpu_count() or 1
     mic = dict(N=cfg.N, pix_size=cfg.pix, Cs=cfg.cs, EkV=cfg.kv, AmpContrast=cfg.ampc)
@@ -682,7 +794,11 @@ def main():
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--config', default='config4')
     ap.add_argument('--n-pd', type=int, default=0, help='override the number of PDs')
-    ap.add_argument('--precision', default='bf16x3', choices=['fp32', 'bf16x3'])
+    ap.add_argument('--precision', default='bf16x3', choices=['fp32', 'bf16x3'],
+                    help='the contraction form of the headline value and e2e')
+    ap.add_argument('--forms', default='fp32,bf16x3',
+                    help='contraction forms timed on the same plan data in the same run '
+                         '(comma list; "" = only --precision)')
     ap.add_argument('--outputs', default='D,img_avg,img_avg_flip,img_all_intensity')
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--no-e2e', action='store_true')
@@ -708,6 +824,13 @@ def main():
     ap.add_argument('--no-precision', action='store_true',
                     help='skip the FP64 / diffusion-map precision report of one sample PD')
     ap.add_argument('--cpu-max-n', type=int, default=900)
+    ap.add_argument('--fullsize-precision', action='store_true',
+                    help='D of the whole first PD against a device FP64 contraction, with '
+                         'near-duplicate and diffusion-map errors (default for config3)')
+    ap.add_argument('--autotune', default='cached', choices=['cached', 'force', ''],
+                    help="contraction schedule per PD size class: the autotuner's cached table "
+                         "(measured first if absent), 'force' = measure again, '' = the "
+                         "library's default schedule")
     ap.add_argument('--no-graph', dest='graph', action='store_false',
                     help='launch the stage directly instead of replaying a captured CUDA graph')
     args = ap.parse_args()
@@ -823,8 +946,29 @@ def main():
         line['dm_embedding'] = r['dm']
     if r.get('nlsa'):
         line['nlsa'] = r['nlsa']
+    if r.get('tuned'):
+        line['contraction_schedule'] = dict(
+            classes=r['tuned'], tuning_s=r['t_tune'],
+            method='manifoldem_python_gb300/autotune.py: per size class, every candidate '
+                   'schedule timed on a synthetic batch of the class (median of 5 executes)')
+    forms = r['forms']
     if not args.no_precision:
-        line['precision'] = precision_report(args, r['ds'], r['counts'], cfg, args.precision)
+        for f in forms:
+            pr = precision_report(args, r['ds'], r['counts'], cfg, f)
+            forms[f]['D_err_vs_fp64_oracle'] = pr['max_rel_err_vs_fp64_oracle']
+            forms[f]['D_err_vs_fp64_contraction'] = pr['max_rel_err_vs_fp64_contraction']
+            forms[f]['dm_top8_subspace_angle_rad'] = pr['dm_top8_subspace_angle_rad']
+            if f == args.precision:
+                line['precision'] = pr
+    line['forms'] = forms
+    if 'fp32' in forms and 'bf16x3' in forms:
+        a, b = forms['fp32'], forms['bf16x3']
+        line['speedup_bf16x3_vs_fp32'] = dict(
+            step=a['ms_per_step'] / b['ms_per_step'],
+            contraction=a['contraction_ms'] / b['contraction_ms'])
+    if args.fullsize_precision or (args.config == 'config3' and not args.no_precision):
+        import torch
+        line['precision_fullsize'] = fullsize_precision(r['ds'], cfg, torch.device('cuda'))
     if not args.no_cpu_baseline:
         cb, _ = cpu_baseline(args, r['ds'], r['counts'], cfg)
         line['cpu_baseline'] = cb

@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define MEM_ABI_VERSION 4
+#define MEM_ABI_VERSION 5
 
 /* status codes */
 #define MEM_OK                    0
@@ -129,6 +129,30 @@ int64_t mem_plan_num_images(const mem_plan* plan);
 int64_t mem_plan_d_elements(const mem_plan* plan);   /* sum n_p^2 */
 int64_t mem_plan_num_pairs(const mem_plan* plan);    /* sum n_p (n_p - 1) / 2 */
 
+/* Schedule of the split-BF16 tensor-core contraction for one size class of PDs: the classes
+ * are given in increasing max_n; a PD of n images belongs to the first class with
+ * n <= max_n (the last class takes every larger PD).  The tiles of each class run in one
+ * launch with the class's schedule.  The reference has no counterpart (its D is one float64
+ * GEMM per PD, modules/getDistanceCTF_local_Conj9combinedS2.py:391-397); the schedules are
+ * picked per box size and class by the autotuner (manifoldem_python_gb300/autotune.py).   */
+typedef struct mem_contraction_config {
+    int32_t max_n;          /* largest PD (images) of the class                                */
+    int32_t persistent;     /* 0: one CTA per 128 x 128 tile; 1: one CTA per SM walking tiles   */
+    int32_t accumulators;   /* TMEM accumulation buffers, 2 or 4 (the MMA issuer may run this
+                               many accumulation groups ahead of the epilogue, across tiles);
+                               2 with 256-wide tiles                                          */
+    int32_t tile_n;         /* D columns per tile: 128, or 256 (128 x 256 tiles: a quarter
+                               fewer operand bytes per MMA, two 96 KB stages instead of three
+                               64 KB ones); 0 means 128                                        */
+} mem_contraction_config;
+
+/* Sets the plan's contraction schedule (HOST array of n_classes >= 1 entries, max_n
+ * strictly increasing); call before mem_plan_upload.  Default: one class, one CTA per tile,
+ * two accumulators, 128-wide tiles.  MEM_ERR_INVALID on a malformed table or after the
+ * upload.                                                                                  */
+int mem_plan_set_contraction(mem_plan* plan, int32_t n_classes,
+                             const mem_contraction_config* classes);
+
 /* Copy the plan's tables into the workspace (stream-ordered).  Call once per workspace
  * before mem_plan_execute (and before capturing it).                                      */
 int mem_plan_upload(mem_plan* plan, void* workspace, size_t workspace_bytes, void* stream);
@@ -153,8 +177,18 @@ int mem_plan_execute_split(mem_plan* plan, const mem_inputs* in, const mem_outpu
                            void* stream);
 
 /* Reads the device status word of the workspace (after the stream has been synchronised):
- * MEM_OK, or MEM_ERR_DEVICE_TIMEOUT if a bounded device-side wait gave up.                 */
+ * MEM_OK; MEM_ERR_DEVICE_TIMEOUT if a bounded device-side wait gave up (the kernel returned
+ * early, its outputs are incomplete); MEM_ERR_INVALID if an entry's stack_index was outside
+ * [0, num_stack) (never dereferenced; that image's outputs are NaN).  The word is cleared at
+ * the start of every execute.                                                              */
 int mem_workspace_status(const mem_plan* plan, const void* workspace);
+
+/* Limit of the bounded device-side waits of the plan's kernels (the tensor-core contraction's
+ * mbarrier waits), in SM clock cycles; default 4e9 (~2 s at 2 GHz), at least 1000.  A wait
+ * that runs out sets the status word's timeout bit, the kernel stops issuing, waits (bounded)
+ * for its own copies and MMAs in flight, frees its tensor memory and returns.  The reference
+ * has no counterpart (it has no device code).  Applies to executes enqueued afterwards.     */
+int mem_plan_set_wait_limit(mem_plan* plan, int64_t cycles);
 
 /* ---- phase timing ------------------------------------------------------------------------
  * When enabled, mem_plan_execute records CUDA events between its phases (gather, lowpass,
@@ -185,8 +219,13 @@ int mem_pd_batch(const mem_params* params, int32_t n_pd, const int32_t* pd_count
  * cudaMalloc, cudaFree or allocating library routine (no cuFFT).
  *   - spectra, df (device, [n]) and D (device, n*n doubles, row-major) are the caller's;
  *     params->avg_only is ignored; params->precision selects the contraction form.
- *   - The first call on a device resolves the array's device address on that device (make it
- *     current first); make that first call before any stream capture.
+ *   - The first call on a device resolves the array's device address and the SM count on that
+ *     device (make it current first); make that first call before any stream capture.  The
+ *     first call on a device and the first call after a change of box size also copy the box
+ *     size's feature-layout tables from host memory into the array; make those calls before
+ *     any stream capture too.  The other per-call tables are written by a kernel.
+ *   - The resolved address assumes the device's context lives until the process exits: a
+ *     cudaDeviceReset between calls is not supported.
  *   - Sizes whose scratch (feature matrix rows padded to 128, spectra copy, sums) would exceed
  *     MEM_NOALLOC_SCRATCH_BYTES return MEM_ERR_TOO_LARGE without launching anything; at 128 px
  *     that allows n <= 187 images, at 70 px n <= 692; boxes above 220 px do not fit.
@@ -196,6 +235,13 @@ int mem_pd_batch(const mem_params* params, int32_t n_pd, const int32_t* pd_count
 #define MEM_NOALLOC_SCRATCH_BYTES (32u << 20)
 int mem_pd_distances_noalloc(const mem_params* params, int32_t n, const float* spectra,
                              const double* df, double* D, void* stream);
+
+/* Status of the last mem_pd_distances_noalloc call on the current device (no counterpart in
+ * the reference; it allocates nothing either): waits for `stream`
+ * (the stream that call was enqueued on), then reads the status word kept at the start of the
+ * static scratch array (no allocation).  MEM_OK, or MEM_ERR_DEVICE_TIMEOUT when a bounded
+ * device-side wait of the split-BF16 contraction gave up (D is then incomplete).           */
+int mem_noalloc_status(void* stream);
 
 /* ---- diffusion-map embedding of one PD's D (the stage's consumer) -----------------------
  * The dense-matrix work of DMembeddingII.op (modules/DMembeddingII.py:86-185) with

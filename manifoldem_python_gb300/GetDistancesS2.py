@@ -53,6 +53,23 @@ def count(N) -> int:
     return N - len(fileCheck())
 
 
+def rank_jobs(input_data: list, N: int, rank: int, world: int) -> list:
+    """This rank's share of the pending jobs (one process per GPU): the longest-processing-
+    time-first partition of the jobs by estimated cost, no data exchange between ranks (the
+    reference scatters its job list over MPI ranks the same way, GetDistancesS2_mpi.py:58-65).
+    Every rank computes the same partition from the same job list, so the shares are disjoint
+    and cover every pending PD."""
+    if world <= 1:
+        return list(input_data)
+    mine = shard([len(j[0]) for j in input_data], int(N), rank, world)
+    return [input_data[i] for i in mine]
+
+
+def world_from_env():
+    """(rank, world size) of a torchrun / MPI-style launch, (0, 1) otherwise."""
+    return int(os.environ.get('RANK', '0')), int(os.environ.get('WORLD_SIZE', '1'))
+
+
 def run_jobs(jobs: list, stack_file: str, nStot: int, options: dict, progress=None,
              budget_bytes: Optional[int] = None, precision: Optional[str] = None,
              done_offset: int = 0, total: Optional[int] = None, writers: int = 4,
@@ -133,19 +150,19 @@ def op(*argv):
         p.nPix = int(np.sqrt(os.path.getsize(p.img_stack_file) / (4 * p.num_part)))
         set_params.op(0)
     input_data = divide(CG, q, df, p.numberofJobs)
-    world = int(os.environ.get('WORLD_SIZE', '1'))
-    if world > 1:
-        # one process per GPU: this rank's LPT share of the pending PDs, no data exchange
-        rank = int(os.environ.get('RANK', '0'))
-        mine = shard([len(j[0]) for j in input_data], int(p.nPix), rank, world)
-        input_data = [input_data[i] for i in mine]
+    rank, world = world_from_env()
+    # one process per GPU: this rank's share of the pending PDs
+    input_data = rank_jobs(input_data, int(p.nPix), rank, world)
     progress = argv[0] if argv else None
     offset = p.numberofJobs - len(input_data)
     if progress is not None:
         progress.emit(int((offset / float(max(p.numberofJobs, 1))) * 100))
     print("Processing {} projection directions.".format(len(input_data)))
     if input_data:
+        # device bytes per admitted batch: p.gpu_budget_bytes when the configuration sets it,
+        # else 60% of the free device memory
         run_jobs(input_data, p.img_stack_file, size, options, progress=progress,
-                 done_offset=offset, total=p.numberofJobs, sh=sh)
+                 budget_bytes=getattr(p, 'gpu_budget_bytes', None), done_offset=offset,
+                 total=p.numberofJobs, sh=sh)
     set_params.op(0)
     return

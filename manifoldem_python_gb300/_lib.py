@@ -112,13 +112,18 @@ class MemParams(ctypes.Structure):
                 ('avg_only', c_int32), ('precision', c_int32)]
 
 
-ABI_VERSION = 4            # MEM_ABI_VERSION of include/manifoldem_gb300.h these structs follow
+ABI_VERSION = 5            # MEM_ABI_VERSION of include/manifoldem_gb300.h these structs follow
 
 
 class MemInputs(ctypes.Structure):
     _fields_ = [('stack', c_void_p), ('num_stack', c_int64), ('stack_index', c_void_p),
                 ('flip', c_void_p), ('psi_rad', c_void_p), ('df', c_void_p),
                 ('shift_yx', c_void_p), ('pd_mask', c_void_p)]
+
+
+class MemContractionConfig(ctypes.Structure):
+    _fields_ = [('max_n', c_int32), ('persistent', c_int32), ('accumulators', c_int32),
+                ('tile_n', c_int32)]
 
 
 class MemOutputs(ctypes.Structure):
@@ -146,6 +151,10 @@ SIGNATURES = {
                                          ctypes.POINTER(MemOutputs), c_void_p, c_size_t, c_void_p,
                                          c_void_p]),
     'mem_workspace_status': (c_int32, [c_void_p, c_void_p]),
+    'mem_plan_set_wait_limit': (c_int32, [c_void_p, c_int64]),
+    'mem_plan_set_contraction': (c_int32, [c_void_p, c_int32,
+                                           ctypes.POINTER(MemContractionConfig)]),
+    'mem_noalloc_status': (c_int32, [c_void_p]),
     'mem_dm_symmetrise': (c_int32, [c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
     'mem_dm_sweep': (c_int32, [c_void_p, c_int64, c_void_p, c_int32, c_double, c_void_p,
                                c_void_p]),

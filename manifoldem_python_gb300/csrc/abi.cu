@@ -262,6 +262,69 @@ CtfConst make_ctf(const mem_params& p, int N) {
     return c;
 }
 
+}  // namespace
+
+void wait_settings_from_env(long long* cycles, int* withhold) {
+    *cycles = kDefaultWaitCycles;
+    *withhold = -1;
+    if (const char* e = std::getenv("MEM_WAIT_CYCLES")) {
+        const long long v = std::atoll(e);
+        if (v >= 1000) *cycles = v;
+    }
+    if (const char* e = std::getenv("MEM_TEST_WITHHOLD_CHUNK")) *withhold = std::atoi(e);
+}
+
+mem_contraction_config default_contraction() {
+    mem_contraction_config c{INT32_MAX, 0, 2, 128};
+    if (const char* e = std::getenv("MEM_TC_PERSISTENT")) c.persistent = std::atoi(e) != 0;
+    if (const char* e = std::getenv("MEM_TC_BUFS")) c.accumulators = std::atoi(e) == 4 ? 4 : 2;
+    if (const char* e = std::getenv("MEM_TC_TILE_N")) c.tile_n = std::atoi(e) == 256 ? 256 : 128;
+    if (c.tile_n == 256) c.accumulators = 2;
+    return c;
+}
+
+int apply_contraction(mem_plan* P, int n_classes, const mem_contraction_config* classes) {
+    if (n_classes < 1 || !classes) return MEM_ERR_INVALID;
+    for (int k = 0; k < n_classes; ++k) {
+        const mem_contraction_config& c = classes[k];
+        if (c.max_n < 1 || (k > 0 && c.max_n <= classes[k - 1].max_n)) return MEM_ERR_INVALID;
+        if (c.persistent != 0 && c.persistent != 1) return MEM_ERR_INVALID;
+        if (c.accumulators != 2 && c.accumulators != 4) return MEM_ERR_INVALID;
+        if (c.tile_n != 0 && c.tile_n != 128 && c.tile_n != 256) return MEM_ERR_INVALID;
+        if (c.tile_n == 256 && c.accumulators != 2) return MEM_ERR_INVALID;
+    }
+    auto cls = [&](int n) {
+        for (int k = 0; k < n_classes - 1; ++k)
+            if (n <= classes[k].max_n) return k;
+        return n_classes - 1;
+    };
+    P->tc_classes.assign(classes, classes + n_classes);
+    for (mem_contraction_config& c : P->tc_classes) {
+        // the compensated epilogue sums of 256-wide tiles would not fit the register file
+        if (c.tile_n != 256 || P->tc_kahan) c.tile_n = 128;
+    }
+    // the tiles of every class, class by class, PDs in plan order: 128-row blocks I and
+    // column blocks J of the class's width that meet the upper triangle (J >= 128 I / width)
+    P->tc_tiles.clear();
+    P->tc_ranges.assign(n_classes, std::make_pair(0, 0));
+    for (int k = 0; k < n_classes; ++k) {
+        const int bn = P->tc_classes[k].tile_n;
+        P->tc_ranges[k].first = (int)P->tc_tiles.size();
+        for (int i = 0; i < P->n_pd; ++i) {
+            const int n = P->pd[i].n;
+            if (cls(n) != k) continue;
+            const int nb = (n + kRowBlock - 1) / kRowBlock, nj = (n + bn - 1) / bn;
+            for (int I = 0; I < nb; ++I)
+                for (int J = (I * kRowBlock) / bn; J < nj; ++J)
+                    P->tc_tiles.push_back(Tile{i, I, J, 0});
+        }
+        P->tc_ranges[k].second = (int)P->tc_tiles.size() - P->tc_ranges[k].first;
+    }
+    return MEM_OK;
+}
+
+namespace {
+
 int check_device(int* device, int* sms) {
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess) {
@@ -366,10 +429,15 @@ int mem_plan_create(const mem_params* params, int32_t n_pd, const int32_t* pd_co
     if (const char* e = std::getenv("MEM_TC_GROUP_CHUNKS")) P->tc_group_chunks = std::atoi(e);
     if (const char* e = std::getenv("MEM_TC_KAHAN")) P->tc_kahan = std::atoi(e) != 0;
     if (const char* e = std::getenv("MEM_TC_TERMS")) P->tc_lolo = std::atoi(e) >= 4;
+    {
+        const mem_contraction_config dc = default_contraction();
+        apply_contraction(P, 1, &dc);
+    }
     // image transforms: the shared-memory FFT kernels where they exist (MEM_SMEM_FFT=0 selects
     // cuFFT, for comparison)
     if (const char* e = std::getenv("MEM_SMEM_FFT")) P->smem_fft = std::atoi(e) != 0;
     P->smem_fft = P->smem_fft && kern::smem_fft_supported(*P);
+    wait_settings_from_env(&P->wait_cycles, &P->test_withhold_chunk);
     if (const char* e = std::getenv("MEM_HOST_LOAD_CTAS")) P->host_load_ctas = std::atoi(e);
     if (const char* e = std::getenv("MEM_HOST_LOAD_THREADS")) {
         const int t = std::atoi(e);
@@ -421,6 +489,7 @@ int mem_plan_create(const mem_params* params, int32_t n_pd, const int32_t* pd_co
     L.img_pd = take(sizeof(int32_t) * P->n_images);
     L.img_row = take(sizeof(int32_t) * P->n_images);
     L.tiles = take(sizeof(Tile) * P->tiles.size());
+    L.tc_tiles = take(sizeof(Tile) * P->tiles.size());   // >= the tiles of any width >= 128
     L.qfix = take(sizeof(uint64_t) * P->n_images);
     L.rotc = take(64 * (size_t)P->n_images);            // two fixed-point rotations per image
     L.gtab = take(sizeof(float) * P->N * P->Nh);
@@ -458,8 +527,15 @@ int64_t mem_plan_num_images(const mem_plan* plan) { return plan ? plan->n_images
 int64_t mem_plan_d_elements(const mem_plan* plan) { return plan ? plan->d_elems : -1; }
 int64_t mem_plan_num_pairs(const mem_plan* plan) { return plan ? plan->n_pairs : -1; }
 
+int mem_plan_set_contraction(mem_plan* plan, int32_t n_classes,
+                             const mem_contraction_config* classes) {
+    if (!plan || plan->uploaded) return MEM_ERR_INVALID;
+    return apply_contraction(plan, n_classes, classes);
+}
+
 int mem_plan_upload(mem_plan* plan, void* workspace, size_t workspace_bytes, void* stream) {
     if (!plan || !workspace) return MEM_ERR_INVALID;
+    plan->uploaded = true;
     if (workspace_bytes < plan->lay.total) return MEM_ERR_WORKSPACE;
     if (plan->device < 0) {
         int st = check_device(&plan->device, &plan->num_sms);
@@ -483,6 +559,11 @@ int mem_plan_upload(mem_plan* plan, void* workspace, size_t workspace_bytes, voi
                                  sizeof(int32_t) * P.n_images, cudaMemcpyHostToDevice, s));
     MEM_CUDA_TRY(cudaMemcpyAsync(at<char>(workspace, L.tiles), P.tiles.data(),
                                  sizeof(Tile) * P.tiles.size(), cudaMemcpyHostToDevice, s));
+    if (P.tc_tiles.size() > P.tiles.size()) return MEM_ERR_INVALID;
+    if (!P.tc_tiles.empty())
+        MEM_CUDA_TRY(cudaMemcpyAsync(at<char>(workspace, L.tc_tiles), P.tc_tiles.data(),
+                                     sizeof(Tile) * P.tc_tiles.size(), cudaMemcpyHostToDevice,
+                                     s));
     MEM_CUDA_TRY(cudaMemcpyAsync(at<char>(workspace, L.colmap), P.ftab.data(),
                                  sizeof(int32_t) * P.ftab.size(), cudaMemcpyHostToDevice, s));
     {
@@ -720,8 +801,9 @@ int execute_impl(mem_plan* plan, const mem_inputs* in, const mem_outputs* out, v
             MEM_STEP(kern::gemm_fp32(P, (const float*)feat_a, pair_norm, scale_bits, tiles, pds,
                                      ft.chunks, out->D, s));
         else
-            MEM_STEP(kern::gemm_split_bf16(P, feat_a, feat_b, pair_norm, scale_bits, tiles, pds,
-                                           ft.chunks, out->D, status, s));
+            MEM_STEP(kern::gemm_split_bf16(P, feat_a, feat_b, pair_norm, scale_bits,
+                                           at<Tile>(ws, L.tc_tiles), pds, ft.chunks, out->D,
+                                           status, s));
     }
     MEM_STEP(mark(9));
 #undef MEM_STEP
@@ -765,7 +847,13 @@ int mem_workspace_status(const mem_plan* plan, const void* workspace) {
     MEM_CUDA_TRY(cudaMemcpy(&st, static_cast<const char*>(workspace) + plan->lay.status,
                             sizeof(st), cudaMemcpyDeviceToHost));
     if (st & kStatusTimeout) return MEM_ERR_DEVICE_TIMEOUT;
-    if (st & 2u) return MEM_ERR_INVALID;
+    if (st & kStatusBadIndex) return MEM_ERR_INVALID;
+    return MEM_OK;
+}
+
+int mem_plan_set_wait_limit(mem_plan* plan, int64_t cycles) {
+    if (!plan || cycles < 1000) return MEM_ERR_INVALID;
+    plan->wait_cycles = (long long)cycles;
     return MEM_OK;
 }
 

@@ -20,6 +20,7 @@
 // (compensated), so the tensor core's FP32 accumulation only ever spans one group.
 // Every mbarrier wait is bounded: on expiry the CTA sets the status word's timeout bit, stops
 // issuing, waits (bounded) for its own TMA copies and MMAs, frees its TMEM and returns.
+#include <algorithm>
 #include <cuda.h>
 #include <type_traits>
 #include <cudaTypedefs.h>
@@ -29,20 +30,31 @@
 namespace mem {
 namespace {
 
-constexpr int TC_M = 128, TC_N = 128, TC_BK = 64, TC_STAGES = 3;
+constexpr int TC_M = 128, TC_BK = 64;
 constexpr int TC_EPI_WARPS = 8;
 constexpr int TC_THREADS = (TC_EPI_WARPS + 2) * 32;
-constexpr int TC_OPB = TC_M * TC_BK * 2;          // one operand tile: 16 KB
-constexpr int TC_STAGE_BYTES = 4 * TC_OPB;        // 64 KB
-constexpr uint32_t TC_TMEM_COLS = 256;            // two 128-column FP32 accumulators
-constexpr size_t TC_SMEM = (size_t)TC_STAGES * TC_STAGE_BYTES + 1024 + 256;
-constexpr long long kWaitCycles = 4000000000ll;   // ~2 s at 2 GHz
+constexpr int TC_OPB = TC_M * TC_BK * 2;          // one 128-row operand box: 16 KB
+constexpr int TC_MAX_STAGES = 3;
+
+// Tile shape 128 x BN (BN = 128 or 256 columns of D): a stage holds A_hi, A_lo (128 rows each)
+// and B_hi, B_lo (BN rows each, BN / 128 boxes) of one 64-wide K chunk; three 64 KB stages
+// at BN = 128, two 96 KB stages at BN = 256
+template <int BN>
+struct TcShape {
+    static constexpr int B_BOXES = BN / 128;
+    static constexpr int STAGE_BYTES = (2 + 2 * B_BOXES) * TC_OPB;
+    static constexpr int STAGES = BN == 256 ? 2 : 3;
+    static constexpr size_t SMEM = (size_t)STAGES * STAGE_BYTES + 1024 + 256;
+    static_assert(STAGES <= TC_MAX_STAGES, "stage ring");
+};
 
 // instruction descriptor, kind::f16: D f32 (bits 4-5 = 1), A bf16 (7-9 = 1), B bf16 (10-12 = 1),
 // K-major A and B (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at bits 24-28, negate B bit 14
-constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TC_N >> 3) << 17) |
-                           ((uint32_t)(TC_M >> 4) << 24);
-constexpr uint32_t IDESC_NEG = IDESC | (1u << 14);
+template <int BN>
+__host__ __device__ constexpr uint32_t idesc_f16() {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+           ((uint32_t)(TC_M >> 4) << 24);
+}
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -75,14 +87,14 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
     return ok != 0;
 }
 
-// bounded wait; false if it expired or another role aborted
+// bounded wait (at most `limit` SM clock cycles); false if it expired or another role aborted
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
-                                          uint32_t* status) {
+                                          uint32_t* status, long long limit) {
     if (mbar_try_wait(bar, parity)) return true;
     const long long t0 = clock64();
     while (!mbar_try_wait(bar, parity)) {
         if (*abort_flag) return false;
-        if (clock64() - t0 > kWaitCycles) {
+        if (clock64() - t0 > limit) {
             *abort_flag = 1;
             atomicOr(status, kStatusTimeout);
             return false;
@@ -92,10 +104,10 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volati
 }
 
 // bounded wait used while draining after an abort (no abort check)
-__device__ __forceinline__ void mbar_drain(uint64_t* bar, uint32_t parity) {
+__device__ __forceinline__ void mbar_drain(uint64_t* bar, uint32_t parity, long long limit) {
     const long long t0 = clock64();
     while (!mbar_try_wait(bar, parity))
-        if (clock64() - t0 > kWaitCycles) return;
+        if (clock64() - t0 > limit) return;
 }
 
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar,
@@ -160,30 +172,48 @@ __device__ __forceinline__ void tmem_ld_wait() {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+constexpr int TC_MAX_BUFS = 4;
+
 struct TcShared {
-    uint64_t full[TC_STAGES];
-    uint64_t empty[TC_STAGES];
-    uint64_t acc_full[2];
-    uint64_t acc_empty[2];
+    uint64_t full[TC_MAX_STAGES];
+    uint64_t empty[TC_MAX_STAGES];
+    uint64_t acc_full[TC_MAX_BUFS];
+    uint64_t acc_empty[TC_MAX_BUFS];
     uint64_t mma_done;
     uint32_t tmem_base;
     int abort_flag;
 };
 
-template <bool KAHAN, bool LOLO>
+// The contraction over the tiles [tile_begin, tile_begin + tile_count) of the plan's tile list:
+// CTA b takes tiles tile_begin + b + k gridDim.x (a persistent CTA when the grid is smaller
+// than the tile count; one tile per CTA when it is as large).  The producer, the MMA issuer and
+// the epilogue each walk the CTA's tiles in the same order; the stage ring and the NBUF TMEM
+// accumulators (NBUF x 128 columns) continue from one tile to the next, so a tile's first
+// groups are loaded and multiplied while the epilogue still adds and stores the previous tile.
+template <bool KAHAN, bool LOLO, int NBUF, int BN>
 __global__ void __launch_bounds__(TC_THREADS, 1) gemm_tc_kernel(
         const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CUtensorMap map_lo,
         const double* __restrict__ pair_norm, const uint32_t* __restrict__ scale_bits,
         const Tile* __restrict__ tiles, const PdDev* __restrict__ pds, double* __restrict__ D,
         uint32_t* __restrict__ status, const int4* __restrict__ chunks, int nchunks,
-        int group_chunks) {
+        int group_chunks, long long wait_limit, int withhold, int tile_begin, int tile_count) {
+    static_assert(NBUF == 2 || NBUF == 4, "two or four TMEM accumulators");
+    static_assert(BN == 128 || BN == 256, "tile widths");
+    static_assert(NBUF * BN <= 512, "TMEM holds 512 columns");
+    using S = TcShape<BN>;
+    constexpr int TC_STAGES = S::STAGES, TC_STAGE_BYTES = S::STAGE_BYTES;
+    constexpr uint32_t IDESC = idesc_f16<BN>(), IDESC_NEG = IDESC | (1u << 14);
+    constexpr int EC = BN / 2;                     // epilogue columns per thread
+    constexpr uint32_t TMEM_COLS = NBUF * BN;
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     TcShared* sh = (TcShared*)(smem + TC_STAGES * TC_STAGE_BYTES);
     volatile int* abort_flag = &sh->abort_flag;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const Tile t = tiles[blockIdx.x];
-    const PdDev pd = pds[t.pd];
+    const int my_tiles = (int)blockIdx.x < tile_count
+                             ? (tile_count - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x
+                             : 0;
+    auto tile_of = [&](int lt) { return tiles[tile_begin + (int)blockIdx.x + lt * (int)gridDim.x]; };
     const int gsize = (group_chunks > 0 && group_chunks < nchunks) ? group_chunks : nchunks;
     const int ngroups = (nchunks + gsize - 1) / gsize;
 
@@ -192,7 +222,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gemm_tc_kernel(
             mbar_init(&sh->full[s], 1);
             mbar_init(&sh->empty[s], 1);
         }
-        for (int b = 0; b < 2; ++b) {
+        for (int b = 0; b < NBUF; ++b) {
             mbar_init(&sh->acc_full[b], 1);
             mbar_init(&sh->acc_empty[b], TC_EPI_WARPS);
         }
@@ -203,7 +233,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gemm_tc_kernel(
     if (warp == TC_EPI_WARPS + 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                          smem_u32(&sh->tmem_base)),
-                     "r"(TC_TMEM_COLS)
+                     "r"(TMEM_COLS)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -211,130 +241,170 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gemm_tc_kernel(
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = sh->tmem_base;
-    const int rowA = (int)(pd.row_off + (int64_t)t.I * TC_M);
-    const int rowB = (int)(pd.row_off + (int64_t)t.J * TC_N);
 
     if (warp == TC_EPI_WARPS) {
         // ---------------------------------------------------------------- TMA producer
         if (lane == 0) {
             asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&map_hi) : "memory");
             asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&map_lo) : "memory");
-            int issued = 0;
-            for (int c = 0; c < nchunks; ++c) {
-                const int st = c % TC_STAGES;
-                const uint32_t ph = (uint32_t)(c / TC_STAGES) & 1u;
-                if (c >= TC_STAGES && !mbar_wait(&sh->empty[st], ph ^ 1u, abort_flag, status))
-                    break;
-                // the chunk schedule interleaves the feature blocks so that the dominant
-                // low-frequency columns of every block are accumulated last
-                const int4 ch = chunks[c];
-                const int ka = ch.x, kb = ch.y;
-                uint8_t* sb = smem + st * TC_STAGE_BYTES;
-                mbar_expect_tx(&sh->full[st], TC_STAGE_BYTES);
-                tma_load_2d(sb + 0 * TC_OPB, &map_hi, &sh->full[st], (int)ka, rowA);
-                tma_load_2d(sb + 1 * TC_OPB, &map_lo, &sh->full[st], (int)ka, rowA);
-                tma_load_2d(sb + 2 * TC_OPB, &map_hi, &sh->full[st], (int)kb, rowB);
-                tma_load_2d(sb + 3 * TC_OPB, &map_lo, &sh->full[st], (int)kb, rowB);
-                issued = c + 1;
+            long long gc = 0, withheld = -1;     // chunks issued by this CTA (all its tiles)
+            bool stop = false;
+            for (int lt = 0; lt < my_tiles && !stop; ++lt) {
+                const Tile t = tile_of(lt);
+                const PdDev pd = pds[t.pd];
+                const int rowA = (int)(pd.row_off + (int64_t)t.I * TC_M);
+                const int rowB = (int)(pd.row_off + (int64_t)t.J * BN);
+                for (int c = 0; c < nchunks; ++c, ++gc) {
+                    const int st = (int)(gc % TC_STAGES);
+                    const uint32_t ph = (uint32_t)(gc / TC_STAGES) & 1u;
+                    if (gc >= TC_STAGES &&
+                        !mbar_wait(&sh->empty[st], ph ^ 1u, abort_flag, status, wait_limit)) {
+                        stop = true;
+                        break;
+                    }
+                    // a withheld chunk (test of the timeout path; first tile only) is never
+                    // loaded, so the MMA issuer's wait for it can only end by its limit
+                    if (lt == 0 && c == withhold) {
+                        withheld = gc;
+                        continue;
+                    }
+                    // the chunk schedule interleaves the feature blocks so that the dominant
+                    // low-frequency columns of every block are accumulated last
+                    const int4 ch = chunks[c];
+                    uint8_t* sb = smem + st * TC_STAGE_BYTES;
+                    mbar_expect_tx(&sh->full[st], TC_STAGE_BYTES);
+                    tma_load_2d(sb + 0 * TC_OPB, &map_hi, &sh->full[st], ch.x, rowA);
+                    tma_load_2d(sb + 1 * TC_OPB, &map_lo, &sh->full[st], ch.x, rowA);
+#pragma unroll
+                    for (int q = 0; q < S::B_BOXES; ++q) {
+                        tma_load_2d(sb + (2 + q) * TC_OPB, &map_hi, &sh->full[st], ch.y,
+                                    rowB + 128 * q);
+                        tma_load_2d(sb + (2 + S::B_BOXES + q) * TC_OPB, &map_lo, &sh->full[st],
+                                    ch.y, rowB + 128 * q);
+                    }
+                }
             }
             if (*abort_flag) {   // let the copies already issued land before the CTA exits
-                for (int c = (issued > TC_STAGES ? issued - TC_STAGES : 0); c < issued; ++c)
-                    mbar_drain(&sh->full[c % TC_STAGES], (uint32_t)(c / TC_STAGES) & 1u);
+                for (long long c = (gc > TC_STAGES ? gc - TC_STAGES : 0); c < gc; ++c)
+                    if (c != withheld)
+                        mbar_drain(&sh->full[c % TC_STAGES], (uint32_t)(c / TC_STAGES) & 1u,
+                                   wait_limit);
             }
         }
     } else if (warp == TC_EPI_WARPS + 1) {
         // ---------------------------------------------------------------- MMA issuer
         if (lane == 0) {
-            bool issued_any = false;
-            int4 ch_next = chunks[0];                   // schedule entry, read one chunk ahead
-            for (int c = 0; c < nchunks; ++c) {
-                const int4 ch = ch_next;
-                if (c + 1 < nchunks) ch_next = chunks[c + 1];
-                const int st = c % TC_STAGES;
-                const uint32_t ph = (uint32_t)(c / TC_STAGES) & 1u;
-                const int g = c / gsize;
-                const int b = g & 1;
-                const bool first = (c % gsize) == 0;
-                const bool last = ((c % gsize) == gsize - 1) || c == nchunks - 1;
-                if (first && g >= 2 &&
-                    !mbar_wait(&sh->acc_empty[b], (uint32_t)((g >> 1) - 1) & 1u, abort_flag,
-                               status))
-                    break;
-                if (!mbar_wait(&sh->full[st], ph, abort_flag, status)) break;
-                tc_fence_after();
-                const bool neg = ch.z != 0;             // r', s' blocks (chunk schedule)
-                const uint32_t idesc = neg ? IDESC_NEG : IDESC;
-                const uint32_t d = tmem + (uint32_t)(b * TC_N);
-                const uint32_t sa = smem_u32(smem + st * TC_STAGE_BYTES);
-                // three products per K step; the lo.lo product too for marked chunks (one
-                // branch per chunk, both bodies fully unrolled)
-                auto mma_chunk = [&](auto four) {
-#pragma unroll
-                    for (int k = 0; k < TC_BK / 16; ++k) {
-                        const uint64_t ahi = sdesc_sw128(sa + 0 * TC_OPB + k * 32);
-                        const uint64_t alo = sdesc_sw128(sa + 1 * TC_OPB + k * 32);
-                        const uint64_t bhi = sdesc_sw128(sa + 2 * TC_OPB + k * 32);
-                        const uint64_t blo = sdesc_sw128(sa + 3 * TC_OPB + k * 32);
-                        umma_bf16(d, ahi, bhi, idesc, (first && k == 0) ? 0u : 1u);
-                        umma_bf16(d, ahi, blo, idesc, 1u);
-                        umma_bf16(d, alo, bhi, idesc, 1u);
-                        if (decltype(four)::value) umma_bf16(d, alo, blo, idesc, 1u);
+            bool issued_any = false, stop = false;
+            long long gc = 0, gg = 0;            // chunks and accumulation groups of this CTA
+            for (int lt = 0; lt < my_tiles && !stop; ++lt) {
+                int4 ch_next = chunks[0];        // schedule entry, read one chunk ahead
+                for (int c = 0; c < nchunks; ++c, ++gc) {
+                    const int4 ch = ch_next;
+                    if (c + 1 < nchunks) ch_next = chunks[c + 1];
+                    const int st = (int)(gc % TC_STAGES);
+                    const uint32_t ph = (uint32_t)(gc / TC_STAGES) & 1u;
+                    const int b = (int)(gg % NBUF);
+                    const long long use = gg / NBUF;        // earlier uses of buffer b
+                    const bool first = (c % gsize) == 0;
+                    const bool last = ((c % gsize) == gsize - 1) || c == nchunks - 1;
+                    if (first && use >= 1 &&
+                        !mbar_wait(&sh->acc_empty[b], (uint32_t)((use - 1) & 1), abort_flag,
+                                   status, wait_limit)) {
+                        stop = true;
+                        break;
                     }
-                };
-                if (LOLO || ch.w != 0)
-                    mma_chunk(std::true_type{});
-                else
-                    mma_chunk(std::false_type{});
-                issued_any = true;
-                umma_commit(&sh->empty[st]);
-                if (last) umma_commit(&sh->acc_full[b]);
+                    if (!mbar_wait(&sh->full[st], ph, abort_flag, status, wait_limit)) {
+                        stop = true;
+                        break;
+                    }
+                    tc_fence_after();
+                    const bool neg = ch.z != 0;             // r', s' blocks (chunk schedule)
+                    const uint32_t idesc = neg ? IDESC_NEG : IDESC;
+                    const uint32_t d = tmem + (uint32_t)(b * BN);
+                    const uint32_t sa = smem_u32(smem + st * TC_STAGE_BYTES);
+                    // three products per K step; the lo.lo product too for marked chunks (one
+                    // branch per chunk, both bodies fully unrolled)
+                    auto mma_chunk = [&](auto four) {
+#pragma unroll
+                        for (int k = 0; k < TC_BK / 16; ++k) {
+                            const uint64_t ahi = sdesc_sw128(sa + 0 * TC_OPB + k * 32);
+                            const uint64_t alo = sdesc_sw128(sa + 1 * TC_OPB + k * 32);
+                            const uint64_t bhi = sdesc_sw128(sa + 2 * TC_OPB + k * 32);
+                            const uint64_t blo =
+                                sdesc_sw128(sa + (2 + S::B_BOXES) * TC_OPB + k * 32);
+                            umma_bf16(d, ahi, bhi, idesc, (first && k == 0) ? 0u : 1u);
+                            umma_bf16(d, ahi, blo, idesc, 1u);
+                            umma_bf16(d, alo, bhi, idesc, 1u);
+                            if (decltype(four)::value) umma_bf16(d, alo, blo, idesc, 1u);
+                        }
+                    };
+                    if (LOLO || ch.w != 0)
+                        mma_chunk(std::true_type{});
+                    else
+                        mma_chunk(std::false_type{});
+                    issued_any = true;
+                    umma_commit(&sh->empty[st]);
+                    if (last) {
+                        umma_commit(&sh->acc_full[b]);
+                        ++gg;
+                    }
+                }
             }
             if (*abort_flag && issued_any) {   // wait for the MMAs in flight
                 umma_commit(&sh->mma_done);
-                mbar_drain(&sh->mma_done, 0);
+                mbar_drain(&sh->mma_done, 0, wait_limit);
             }
         }
     } else {
         // ---------------------------------------------------------------- epilogue
         const int q = warp & 3, h = warp >> 2;
         const int row = q * 32 + lane;
-        float acc[64], cmp[64];
-#pragma unroll
-        for (int j = 0; j < 64; ++j) acc[j] = cmp[j] = 0.f;
         bool ok = true;
-        for (int g = 0; g < ngroups && ok; ++g) {
-            const int b = g & 1;
-            ok = mbar_wait(&sh->acc_full[b], (uint32_t)(g >> 1) & 1u, abort_flag, status);
-            __syncwarp();
-            ok = __all_sync(0xffffffffu, ok);
-            if (!ok) break;
-            tc_fence_after();
-            const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * TC_N + h * 64);
+        long long gg = 0;
+        for (int lt = 0; lt < my_tiles && ok; ++lt) {
+            const Tile t = tile_of(lt);
+            float acc[EC], cmp[KAHAN ? EC : 1];
 #pragma unroll
-            for (int half = 0; half < 2; ++half) {
-                uint32_t r[32];
-                tmem_ld32(taddr + half * 32, r);
-                tmem_ld_wait();
+            for (int j = 0; j < EC; ++j) acc[j] = 0.f;
 #pragma unroll
-                for (int j = 0; j < 32; ++j) {
-                    const float x = __uint_as_float(r[j]);
-                    float& s = acc[half * 32 + j];
-                    if (KAHAN) {
-                        float& c = cmp[half * 32 + j];
-                        const float y = x - c;
-                        const float tt = s + y;
-                        c = (tt - s) - y;
-                        s = tt;
-                    } else {
-                        s += x;
+            for (int j = 0; j < (KAHAN ? EC : 1); ++j) cmp[j] = 0.f;
+            for (int g = 0; g < ngroups; ++g, ++gg) {
+                const int b = (int)(gg % NBUF);
+                const long long use = gg / NBUF;
+                ok = mbar_wait(&sh->acc_full[b], (uint32_t)(use & 1), abort_flag, status,
+                               wait_limit);
+                __syncwarp();
+                ok = __all_sync(0xffffffffu, ok);
+                if (!ok) break;
+                tc_fence_after();
+                const uint32_t taddr =
+                    tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN + h * EC);
+#pragma unroll
+                for (int half = 0; half < EC / 32; ++half) {
+                    uint32_t r[32];
+                    tmem_ld32(taddr + half * 32, r);
+                    tmem_ld_wait();
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) {
+                        const float x = __uint_as_float(r[j]);
+                        float& s = acc[half * 32 + j];
+                        if (KAHAN) {
+                            float& c = cmp[KAHAN ? half * 32 + j : 0];
+                            const float y = x - c;
+                            const float tt = s + y;
+                            c = (tt - s) - y;
+                            s = tt;
+                        } else {
+                            s += x;
+                        }
                     }
                 }
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&sh->acc_empty[b]);
             }
-            tc_fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&sh->acc_empty[b]);
-        }
-        if (ok && !*abort_flag) {
+            if (!ok || *abort_flag) break;
+            const PdDev pd = pds[t.pd];
             const double sc = (double)feature_scale_from_bits(scale_bits[t.pd]);
             const double inv_sc2 = 1.0 / (sc * sc);
             const int n = pd.n;
@@ -343,16 +413,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gemm_tc_kernel(
             const double* an = pair_norm + pd.img_off;
             if (gi < n) {
                 const double ai = an[gi];
-                const int j0 = t.J * TC_N + h * 64;
+                const int j0 = t.J * BN + h * EC;
 #pragma unroll
-                for (int j = 0; j < 64; ++j) {
+                for (int j = 0; j < EC; ++j) {
                     const int gj = j0 + j;
                     if (gj >= n || gj < gi) continue;
                     if (gj == gi) {
                         Dp[(int64_t)gi * n + gi] = 0.0;
                         continue;
                     }
-                    const float e = KAHAN ? (acc[j] - cmp[j]) : acc[j];
+                    const float e = KAHAN ? (acc[j] - cmp[KAHAN ? j : 0]) : acc[j];
                     const double v = ai + an[gj] + (double)e * inv_sc2;
                     Dp[(int64_t)gi * n + gj] = v;
                     Dp[(int64_t)gj * n + gi] = v;
@@ -365,7 +435,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gemm_tc_kernel(
     if (warp == TC_EPI_WARPS + 1) {
         tc_fence_after();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
-                     "r"(TC_TMEM_COLS)
+                     "r"(TMEM_COLS)
                      : "memory");
     }
 }
@@ -413,22 +483,39 @@ int gemm_split_bf16(const mem_plan& P, const void* feat_hi, const void* feat_lo,
     if (st != MEM_OK) return st;
     st = make_map(&mlo, feat_lo, P.Kf, P.n_rows);
     if (st != MEM_OK) return st;
-#define MEM_TC_LAUNCH(KAHAN, LOLO)                                                             \
+    const int sms = P.num_sms > 0 ? P.num_sms : 1;
+    // one launch per size class of the plan's contraction configuration (tiles sorted by class)
+    for (size_t k = 0; k < P.tc_ranges.size(); ++k) {
+        const int begin = P.tc_ranges[k].first, count = P.tc_ranges[k].second;
+        if (count <= 0) continue;
+        const mem_contraction_config& cfg = P.tc_classes[k];
+        const unsigned grid = cfg.persistent ? (unsigned)std::min(count, sms) : (unsigned)count;
+#define MEM_TC_LAUNCH(KAHAN, LOLO, NB, BN)                                                     \
     do {                                                                                       \
-        MEM_CUDA_TRY(cudaFuncSetAttribute(gemm_tc_kernel<KAHAN, LOLO>,                         \
+        MEM_CUDA_TRY(cudaFuncSetAttribute(gemm_tc_kernel<KAHAN, LOLO, NB, BN>,                 \
                                           cudaFuncAttributeMaxDynamicSharedMemorySize,         \
-                                          (int)TC_SMEM));                                      \
-        gemm_tc_kernel<KAHAN, LOLO><<<(unsigned)P.tiles.size(), TC_THREADS, TC_SMEM, s>>>(     \
+                                          (int)TcShape<BN>::SMEM));                            \
+        gemm_tc_kernel<KAHAN, LOLO, NB, BN><<<grid, TC_THREADS, TcShape<BN>::SMEM, s>>>(       \
             mhi, mlo, pair_norm, scale_bits, tiles, pds, D, status, chunks, P.n_chunks,        \
-            P.tc_group_chunks);                                                                \
+            P.tc_group_chunks, P.wait_cycles, P.test_withhold_chunk, begin, count);            \
     } while (0)
-    if (P.tc_kahan) {
-        if (P.tc_lolo) MEM_TC_LAUNCH(true, true); else MEM_TC_LAUNCH(true, false);
-    } else {
-        if (P.tc_lolo) MEM_TC_LAUNCH(false, true); else MEM_TC_LAUNCH(false, false);
-    }
+#define MEM_TC_SHAPE(KAHAN, LOLO)                                                              \
+    do {                                                                                       \
+        if (cfg.tile_n == 256) MEM_TC_LAUNCH(KAHAN, LOLO, 2, 256);                             \
+        else if (cfg.accumulators == 4) MEM_TC_LAUNCH(KAHAN, LOLO, 4, 128);                    \
+        else MEM_TC_LAUNCH(KAHAN, LOLO, 2, 128);                                               \
+    } while (0)
+        // the compensated sums of the 256-wide tile would not fit the register file: its
+        // classes keep the 128-wide kernel (apply_contraction) when MEM_TC_KAHAN is set
+        if (P.tc_kahan) {
+            if (P.tc_lolo) MEM_TC_LAUNCH(true, true, 2, 128); else MEM_TC_LAUNCH(true, false, 2, 128);
+        } else {
+            if (P.tc_lolo) MEM_TC_SHAPE(false, true); else MEM_TC_SHAPE(false, false);
+        }
+#undef MEM_TC_SHAPE
 #undef MEM_TC_LAUNCH
-    MEM_LAUNCH_CHECK();
+        MEM_LAUNCH_CHECK();
+    }
     return MEM_OK;
 }
 }  // namespace kern

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <cufft.h>
 #include <cstdint>
+#include <utility>
 #include <vector>
 
 #include "../../include/manifoldem_gb300.h"
@@ -19,6 +20,12 @@ constexpr int kFftChunk = 8192;     // images per batched cuFFT execution
 
 // device status word bits (first 4 bytes of the workspace)
 constexpr uint32_t kStatusTimeout = 1u;
+constexpr uint32_t kStatusBadIndex = 2u;
+constexpr long long kDefaultWaitCycles = 4000000000ll;   // ~2 s at 2 GHz
+
+// wait limit and withheld chunk from MEM_WAIT_CYCLES / MEM_TEST_WITHHOLD_CHUNK (tests of the
+// timeout path); defaults otherwise
+void wait_settings_from_env(long long* cycles, int* withhold);
 
 // ---- per-PD table uploaded to the workspace --------------------------------------------
 struct PdDev {
@@ -37,7 +44,8 @@ struct SumItem {
     int64_t img_begin, img_end;
 };
 
-// D contraction tile: PD pd, row block I, column block J (I <= J)
+// D contraction tile: PD pd, 128-row block I, column block J of the tile's width (128 for the
+// FP32 form; 128 or 256 for the split-BF16 form's classes)
 struct Tile {
     int32_t pd, I, J, pad;
 };
@@ -75,7 +83,7 @@ struct FeatTables {
 };
 
 struct Layout {
-    size_t status, pd_table, sum_items, img_pd, img_row, tiles;
+    size_t status, pd_table, sum_items, img_pd, img_row, tiles, tc_tiles;
     size_t item_off, qfix, rotc, gtab, pd_max, colmap, twid, ident;
     size_t xbuf, spec, feat_a, feat_b, pair_norm, partial, means, avg_spec, avg_real, cufft_work;
     size_t total;
@@ -109,6 +117,12 @@ struct mem_plan {
     size_t cufft_work_bytes = 0;
     int device = -1;
     int num_sms = 0;
+    // contraction schedule per size class (mem_plan_set_contraction) and each class's range of
+    // the tile list (tiles sorted by class): (first tile, tile count)
+    std::vector<mem_contraction_config> tc_classes;
+    std::vector<std::pair<int, int>> tc_ranges;
+    std::vector<mem::Tile> tc_tiles;   // the split-BF16 contraction's tiles (J in tile_n units)
+    bool uploaded = false;
     int tc_group_chunks = 1;        // 64-wide K chunks per TMEM accumulation group (0 = all)
     bool tc_kahan = false;          // compensated register sums across groups
     bool tc_lolo = false;           // add the lo.lo product (4-term split)
@@ -119,6 +133,12 @@ struct mem_plan {
     int host_load_ctas = 8;
     int host_load_threads = 1024;   // 256, 512 or 1024
                                     // with the stack in host memory
+    // bounded device-side waits (the tcgen05 contraction's mbarrier waits) give up after this
+    // many SM clock cycles (~2 s at 2 GHz) and set the status word's timeout bit
+    long long wait_cycles = mem::kDefaultWaitCycles;
+    // test of the timeout path only: the contraction's producer never loads this chunk (-1: none),
+    // so the wait for it can only end by the limit above
+    int test_withhold_chunk = -1;
     bool timing = false;
     bool timed_run = false;
     cudaEvent_t ev[MEM_NUM_PHASES + 1] = {};
@@ -198,6 +218,13 @@ int gemm_split_bf16(const mem_plan& P, const void* feat_hi, const void* feat_lo,
 }  // namespace kern
 
 std::vector<int32_t> radius_descending_columns(int N, int64_t Kc, int64_t Kc_pad);
+
+// default contraction schedule: one class, one CTA per 128 x 128 tile, two TMEM accumulators
+// (MEM_TC_PERSISTENT / MEM_TC_BUFS / MEM_TC_TILE_N override it, for tuning)
+mem_contraction_config default_contraction();
+
+// orders the plan's tiles by size class and sets tc_classes / tc_ranges
+int apply_contraction(mem_plan* P, int n_classes, const mem_contraction_config* classes);
 
 // largest half-plane size for ring features (the features kernel keeps one float per frequency
 // in shared memory); larger boxes use per-frequency U', V' blocks

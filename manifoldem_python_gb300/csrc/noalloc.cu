@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
+#include <mutex>
 #include <vector>
 
 #include "mem_internal.cuh"
@@ -23,15 +24,44 @@ namespace {
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[MEM_NOALLOC_SCRATCH_BYTES];
 
-// device address of the scratch array, looked up once per device
+// per device: the scratch array's device address and the SM count, resolved once (first call on
+// the device, with the device current); the feature-layout tables resident in the array (box
+// size and ring setting of the copy there, -1 = none)
 constexpr int kMaxDevices = 64;
-void* g_scratch_ptr[kMaxDevices] = {};
+struct DeviceSlot {
+    std::once_flag once;
+    int err = cudaSuccess;
+    void* ptr = nullptr;
+    int sms = 0;
+    std::mutex mu;              // guards the resident-table record
+    long long ftab_key = -1;
+};
+DeviceSlot g_slot[kMaxDevices];
+
+int resolve_device(int dev, DeviceSlot** out) {
+    DeviceSlot& d = g_slot[dev];
+    std::call_once(d.once, [&d, dev]() {
+        void* ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        int sms = 0;
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        d.err = (int)e;
+        d.ptr = ptr;
+        d.sms = sms;
+    });
+    if (d.err != cudaSuccess || !d.ptr) return MEM_ERR_CUDA;
+    *out = &d;
+    return MEM_OK;
+}
 
 size_t a256(size_t x) { return (x + 255) / 256 * 256; }
 
+// The array's layout: the status word, the feature-layout tables (a function of the box size
+// only, at a fixed offset so that a copy stays valid for later calls with the same box size),
+// then the per-call tables and buffers.
 struct NoallocLayout {
-    size_t status, pd_table, items, item_off, img_pd, img_row, tiles, qfix, partial, means,
-        avg_spec, pd_max, colmap, spec, feat_a, feat_b, pair_norm, total;
+    size_t status, colmap, pd_table, items, item_off, img_pd, img_row, tiles, qfix, partial, means,
+        avg_spec, pd_max, spec, feat_a, feat_b, pair_norm, total;
 };
 
 NoallocLayout layout_for(const mem_plan& P) {
@@ -44,6 +74,7 @@ NoallocLayout layout_for(const mem_plan& P) {
     };
     const size_t feat_elem = (P.params.precision == MEM_PREC_FP32) ? 4 : 2;
     L.status = take(16);
+    L.colmap = take(sizeof(int32_t) * P.ftab.size());
     L.pd_table = take(sizeof(PdDev));
     L.items = take(sizeof(SumItem) * P.items.size());
     L.item_off = take(sizeof(int32_t) * 2);
@@ -55,13 +86,52 @@ NoallocLayout layout_for(const mem_plan& P) {
     L.means = take(sizeof(float) * means_stride(P));
     L.avg_spec = take(sizeof(float) * 4 * P.Kc);
     L.pd_max = take(sizeof(uint32_t));
-    L.colmap = take(sizeof(int32_t) * P.ftab.size());
     L.spec = take(sizeof(float) * 2 * P.Kc * P.n_images);
     L.feat_a = take(feat_elem * P.Kf * P.n_rows);
     L.feat_b = (feat_elem == 4) ? L.feat_a : take(feat_elem * P.Kf * P.n_rows);
     L.pair_norm = take(sizeof(double) * P.n_images);
     L.total = off;
     return L;
+}
+
+// FNV-1a hash of the feature-layout tables: identifies the copy resident in the array
+long long ftab_hash(const std::vector<int32_t>& t) {
+    uint64_t h = 1469598103934665603ull;
+    for (int32_t v : t) {
+        h ^= (uint32_t)v;
+        h *= 1099511628211ull;
+    }
+    return (long long)(h & 0x7fffffffffffffffull);
+}
+
+// the per-call tables of a one-PD plan of n images, written on the device (no host copy):
+// the PD, the partial-sum items of kSumChunk images, image -> (PD, feature row), and the
+// upper-triangle tiles (I, J), I <= J < nb, in the host plan's order (I outer)
+__global__ void noalloc_tables_kernel(PdDev* __restrict__ pd, SumItem* __restrict__ items,
+                                      int32_t* __restrict__ item_off, int32_t* __restrict__ img_pd,
+                                      int32_t* __restrict__ img_row, Tile* __restrict__ tiles,
+                                      int n, int n_items, int nb, int n_tiles) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t == 0) {
+        *pd = PdDev{0, 0, 0, n, 0, 1.0, 0.0};
+        item_off[0] = 0;
+        item_off[1] = n_items;
+    }
+    if (t < n) {
+        img_pd[t] = 0;
+        img_row[t] = t;
+    }
+    if (t < n_items)
+        items[t] = SumItem{0, 0, (int64_t)t * kSumChunk,
+                           min((int64_t)n, (int64_t)(t + 1) * kSumChunk)};
+    if (t < n_tiles) {
+        int I = 0, rem = t;
+        while (rem >= nb - I) {
+            rem -= nb - I;
+            ++I;
+        }
+        tiles[t] = Tile{0, I, I + rem, 0};
+    }
 }
 
 // host tables of a one-PD plan (no cuFFT plans, no device queries beyond the SM count)
@@ -73,11 +143,16 @@ void one_pd_tables(mem_plan& P, const mem_params& prm, int n) {
     P.Kc = (int64_t)P.N * P.Nh;
     if (const char* e = std::getenv("MEM_RING_FEATURES")) P.ring_features = std::atoi(e) != 0;
     feature_layout(&P);
+    wait_settings_from_env(&P.wait_cycles, &P.test_withhold_chunk);
     P.count.assign(1, n);
     P.pd.assign(1, PdDev{0, 0, 0, n, 0, 1.0, 0.0});
     const int nb = (n + kRowBlock - 1) / kRowBlock;
     for (int I = 0; I < nb; ++I)
         for (int J = I; J < nb; ++J) P.tiles.push_back(Tile{0, I, J, 0});
+    // the tile table is written by noalloc_tables_kernel: 128-wide tiles
+    mem_contraction_config dc = default_contraction();
+    dc.tile_n = 128;
+    apply_contraction(&P, 1, &dc);
     for (int64_t b = 0; b < n; b += kSumChunk)
         P.items.push_back(SumItem{0, 0, b, std::min<int64_t>(n, b + kSumChunk)});
     for (int k = 0; k < n; ++k) {
@@ -130,35 +205,35 @@ extern "C" int mem_pd_distances_noalloc(const mem_params* params, int32_t n, con
     int dev = -1;
     MEM_CUDA_TRY(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kMaxDevices) return MEM_ERR_INVALID;
-    if (!g_scratch_ptr[dev]) {
-        // first call on this device: resolve the device address of the static scratch array
-        void* ptr = nullptr;
-        MEM_CUDA_TRY(cudaGetSymbolAddress(&ptr, g_noalloc_scratch));
-        g_scratch_ptr[dev] = ptr;
-    }
-    cudaDeviceProp prop;
-    MEM_CUDA_TRY(cudaGetDeviceProperties(&prop, dev));
+    DeviceSlot* slot = nullptr;
+    int st = resolve_device(dev, &slot);
+    if (st != MEM_OK) return st;
     P.device = dev;
-    P.num_sms = prop.multiProcessorCount;
-    void* ws = g_scratch_ptr[dev];
+    P.num_sms = slot->sms;
+    void* ws = slot->ptr;
     cudaStream_t s = (cudaStream_t)stream;
 
-    std::vector<int32_t> item_off = {0, (int32_t)P.items.size()};
     MEM_CUDA_TRY(cudaMemsetAsync(at<char>(ws, L.status), 0, 16, s));
-    MEM_CUDA_TRY(cudaMemcpyAsync(at<char>(ws, L.pd_table), P.pd.data(), sizeof(PdDev),
-                                 cudaMemcpyHostToDevice, s));
-    MEM_CUDA_TRY(cudaMemcpyAsync(at<char>(ws, L.items), P.items.data(),
-                                 sizeof(SumItem) * P.items.size(), cudaMemcpyHostToDevice, s));
-    MEM_CUDA_TRY(cudaMemcpyAsync(at<char>(ws, L.item_off), item_off.data(), sizeof(int32_t) * 2,
-                                 cudaMemcpyHostToDevice, s));
-    MEM_CUDA_TRY(cudaMemcpyAsync(at<char>(ws, L.img_pd), P.img_pd.data(), sizeof(int32_t) * n,
-                                 cudaMemcpyHostToDevice, s));
-    MEM_CUDA_TRY(cudaMemcpyAsync(at<char>(ws, L.img_row), P.img_row.data(), sizeof(int32_t) * n,
-                                 cudaMemcpyHostToDevice, s));
-    MEM_CUDA_TRY(cudaMemcpyAsync(at<char>(ws, L.tiles), P.tiles.data(),
-                                 sizeof(Tile) * P.tiles.size(), cudaMemcpyHostToDevice, s));
-    MEM_CUDA_TRY(cudaMemcpyAsync(at<char>(ws, L.colmap), P.ftab.data(),
-                                 sizeof(int32_t) * P.ftab.size(), cudaMemcpyHostToDevice, s));
+    {
+        // the feature-layout tables: copied from the host only when the array holds another
+        // box size's (first call on the device or a change of box size)
+        std::lock_guard<std::mutex> lk(slot->mu);
+        const long long key = ftab_hash(P.ftab);
+        if (slot->ftab_key != key) {
+            MEM_CUDA_TRY(cudaMemcpyAsync(at<char>(ws, L.colmap), P.ftab.data(),
+                                         sizeof(int32_t) * P.ftab.size(), cudaMemcpyHostToDevice,
+                                         s));
+            slot->ftab_key = key;
+        }
+    }
+    const int nb = (n + kRowBlock - 1) / kRowBlock;
+    const int n_items = (int)P.items.size(), n_tiles = (int)P.tiles.size();
+    const int fill = std::max(n, std::max(n_items, n_tiles));
+    noalloc_tables_kernel<<<(fill + 255) / 256, 256, 0, s>>>(
+        at<PdDev>(ws, L.pd_table), at<SumItem>(ws, L.items), at<int32_t>(ws, L.item_off),
+        at<int32_t>(ws, L.img_pd), at<int32_t>(ws, L.img_row), at<Tile>(ws, L.tiles), n, n_items,
+        nb, n_tiles);
+    MEM_LAUNCH_CHECK();
     // the feature kernel overwrites its spectrum with sign(C) F: work on a copy in the scratch
     MEM_CUDA_TRY(cudaMemcpyAsync(at<char>(ws, L.spec), spectra, sizeof(float) * 2 * P.Kc * n,
                                  cudaMemcpyDeviceToDevice, s));
@@ -174,7 +249,6 @@ extern "C" int mem_pd_distances_noalloc(const mem_params* params, int32_t n, con
     }
     mem_inputs in{};
     in.df = df;
-    int st;
 #define NA_STEP(x)                   \
     do {                             \
         st = (x);                    \
@@ -204,5 +278,19 @@ extern "C" int mem_pd_distances_noalloc(const mem_params* params, int32_t n, con
                                       pair_norm, scale_bits, at<Tile>(ws, L.tiles), pds,
                                       ft.chunks, D, at<uint32_t>(ws, L.status), s));
 #undef NA_STEP
+    return MEM_OK;
+}
+
+extern "C" int mem_noalloc_status(void* stream) {
+    int dev = -1;
+    MEM_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return MEM_ERR_INVALID;
+    DeviceSlot* slot = nullptr;
+    const int st = resolve_device(dev, &slot);
+    if (st != MEM_OK) return st;
+    MEM_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+    uint32_t word = 0;
+    MEM_CUDA_TRY(cudaMemcpy(&word, slot->ptr, sizeof(word), cudaMemcpyDeviceToHost));
+    if (word & kStatusTimeout) return MEM_ERR_DEVICE_TIMEOUT;
     return MEM_OK;
 }

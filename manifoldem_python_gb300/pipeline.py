@@ -61,7 +61,10 @@ class Plan:
     """A C-ABI plan plus its torch-allocated workspace, reusable across executions."""
 
     def __init__(self, params: StageParams, counts: Sequence[int], psi_p: Sequence[float],
-                 device=None):
+                 device=None, contraction=None):
+        """``contraction``: the split-BF16 contraction's schedule per size class (a list of
+        dicts max_n / persistent / accumulators, see ``autotune``); default: the autotuner's
+        cached table for this GPU and box size if there is one, else the library's default."""
         import torch
         self.lib = _lib.load()
         self.params = params
@@ -76,6 +79,16 @@ class Plan:
                                                 self.counts.ctypes.data, self.psi_p.ctypes.data,
                                                 ctypes.byref(h)), 'mem_plan_create')
         self.handle = h
+        if contraction is None and params.precision == 'bf16x3':
+            from . import autotune
+            contraction = autotune.lookup(torch.cuda.get_device_name(self.device), params.N,
+                                          params.precision)
+        self.contraction = contraction
+        if contraction:
+            from . import autotune
+            arr = autotune.to_c(contraction)
+            _lib.check(self.lib.mem_plan_set_contraction(h, len(contraction), arr),
+                       'mem_plan_set_contraction')
         sz = ctypes.c_size_t()
         _lib.check(self.lib.mem_plan_workspace_size(h, ctypes.byref(sz)), 'workspace_size')
         self.ws_bytes = int(sz.value)

@@ -182,12 +182,11 @@ def particle_counts(cfg: SynthConfig) -> np.ndarray:
     return _particle_counts(cfg, np.random.default_rng(cfg.seed))
 
 
-def make_dataset(cfg: SynthConfig, device="cpu", dtype=None, pd_limit: Optional[int] = None,
-                 pd_select: Optional[Sequence[int]] = None) -> Dataset:
-    """Build the dataset of ``cfg``.  ``pd_limit`` keeps only the first PDs; ``pd_select`` keeps
-    the listed PDs of the full workload (same geometry), rendering only their particles."""
-    import torch
-
+def make_geometry(cfg: SynthConfig, pd_limit: Optional[int] = None) -> dict:
+    """Everything of the dataset of ``cfg`` except the images: particle counts, orientations,
+    defoci, latent coordinates, near-duplicates, the blob volume and the noise seed (host
+    arrays).  ``make_dataset`` renders from it; a workload too large for one device renders it
+    PD batch by PD batch with ``render_pds``.  ``pd_limit`` keeps only the first PDs."""
     rng = np.random.default_rng(cfg.seed)
     counts = _particle_counts(cfg, rng)
     n_pd = cfg.n_pd if pd_limit is None else min(pd_limit, cfg.n_pd)
@@ -251,6 +250,26 @@ def make_dataset(cfg: SynthConfig, device="cpu", dtype=None, pd_limit: Optional[
     moves *= (0.15 * N) / np.linalg.norm(moves, axis=0)
     noise_seed = int(rng.integers(0, 2**62))
 
+    return dict(CG=CG, q_orig=q_orig, df_orig=df_orig, latent=latent, near_dup_of=near_dup_of,
+                num_part=num_part, radii=radii, centre=centre, amp=amp, moves=moves,
+                noise_seed=noise_seed)
+
+
+def make_dataset(cfg: SynthConfig, device="cpu", dtype=None, pd_limit: Optional[int] = None,
+                 pd_select: Optional[Sequence[int]] = None) -> Dataset:
+    """Build the dataset of ``cfg``.  ``pd_limit`` keeps only the first PDs; ``pd_select`` keeps
+    the listed PDs of the full workload (same geometry), rendering only their particles."""
+    return render_pds(cfg, make_geometry(cfg, pd_limit), pd_select, device, dtype)
+
+
+def render_pds(cfg: SynthConfig, geom: dict, pd_select: Optional[Sequence[int]] = None,
+               device="cpu", dtype=None) -> Dataset:
+    """The dataset of the PDs ``pd_select`` (all when None) of a geometry from
+    ``make_geometry``: their particles rendered on ``device``, indices remapped to them."""
+    CG, q_orig, df_orig = geom['CG'], geom['q_orig'], geom['df_orig']
+    latent, near_dup_of, num_part = geom['latent'], geom['near_dup_of'], geom['num_part']
+    radii, centre, amp, moves = geom['radii'], geom['centre'], geom['amp'], geom['moves']
+    noise_seed = geom['noise_seed']
     if pd_select is not None:
         sel = [int(i) for i in pd_select]
         phys = [np.where(CG[i] >= num_part, CG[i] - num_part, CG[i]) for i in sel]

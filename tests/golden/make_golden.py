@@ -1,7 +1,8 @@
 """Generate the golden fixtures of the distance stage by running the reference itself.
 
-Run in a container that has the reference checkout at /root/reference (read-only); the GPU host
-never runs this.  For each case it writes a seeded synthetic SPIDER stack (values rounded to
+Run in a container that has a checkout of the reference (read-only); its ``modules`` directory
+is given by ``--ref-modules DIR`` or the environment variable MANIFOLDEM_REF_MODULES.  The GPU
+host never runs this.  For each case it writes a seeded synthetic SPIDER stack (values rounded to
 float16 so the fixture can store them exactly at half size), runs the reference's
 ``getDistanceCTF_local_Conj9combinedS2.op`` on it through the reference's own module globals,
 reads back the pickle it writes, and stores inputs and outputs in ``tests/golden/<case>.npz``.
@@ -10,7 +11,7 @@ The reference imports matplotlib and mrcfile (absent here) and uses ``np.complex
 (removed from numpy 2); the loader installs empty stand-ins for the two modules and restores the
 two aliases before importing.  Nothing else of the reference is changed.
 
-Usage:  python tests/golden/make_golden.py [case ...]
+Usage:  python tests/golden/make_golden.py --ref-modules <reference>/modules [case ...]
 """
 from __future__ import annotations
 
@@ -25,7 +26,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF_MODULES = '/root/reference/modules'
+REF_MODULES = os.environ.get('MANIFOLDEM_REF_MODULES', '')
 
 
 def load_reference():
@@ -302,7 +303,16 @@ def make_trim_case(name):
 
 
 if __name__ == '__main__':
-    names = sys.argv[1:] or list(CASES) + list(NLSA_CASES) + list(TRIM_CASES)
+    import argparse
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--ref-modules', default=REF_MODULES,
+                    help="the reference's modules directory (or MANIFOLDEM_REF_MODULES)")
+    ap.add_argument('cases', nargs='*')
+    a = ap.parse_args()
+    if not a.ref_modules or not os.path.isdir(a.ref_modules):
+        sys.exit('give the reference modules directory: --ref-modules DIR')
+    REF_MODULES = a.ref_modules
+    names = a.cases or list(CASES) + list(NLSA_CASES) + list(TRIM_CASES)
     for n in names:
         if n in NLSA_CASES:
             make_nlsa_case(n)

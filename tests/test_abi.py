@@ -88,3 +88,27 @@ def test_invalid_arguments(lib):
     assert _plan(lib, bad, [5], [1.0])[0] == _lib.MEM_ERR_INVALID
     assert lib.mem_plan_execute(None, None, None, None, 0, None) == _lib.MEM_ERR_INVALID
     assert lib.mem_status_string(_lib.MEM_ERR_WORKSPACE) == b'workspace too small'
+
+
+def test_contraction_schedule_table_is_validated(lib):
+    """mem_plan_set_contraction: increasing max_n, persistent 0/1, 2 or 4 accumulators, and
+    only before the upload (no GPU needed)."""
+    P = StageParams(N=64, pix_size=2.0, Cs=2.7, EkV=300.0, AmpContrast=0.1,
+                    precision='bf16x3').to_c()
+    st, h = _plan(lib, P, [300, 129, 1, 900], [10.0, 20.0, 30.0, 40.0])
+    assert st == 0
+    C = _lib.MemContractionConfig
+    try:
+        good = (C * 3)(C(200, 0, 2, 0), C(640, 1, 4, 128), C(2 ** 31 - 1, 1, 2, 256))
+        assert lib.mem_plan_set_contraction(h, 3, good) == _lib.MEM_OK
+        for bad in ((C * 2)(C(640, 1, 2, 0), C(200, 1, 2, 0)),      # not increasing
+                    (C * 2)(C(200, 2, 2, 0), C(640, 1, 2, 0)),      # persistent not 0/1
+                    (C * 2)(C(200, 1, 3, 0), C(640, 1, 2, 0)),      # 3 accumulators
+                    (C * 2)(C(200, 1, 2, 64), C(640, 1, 2, 0)),     # 64-wide tiles
+                    (C * 2)(C(200, 1, 4, 256), C(640, 1, 2, 0))):   # 4 x 256 TMEM columns
+            assert lib.mem_plan_set_contraction(h, 2, bad) == _lib.MEM_ERR_INVALID
+        assert lib.mem_plan_set_contraction(h, 0, good) == _lib.MEM_ERR_INVALID
+        assert lib.mem_plan_set_wait_limit(h, 999) == _lib.MEM_ERR_INVALID
+        assert lib.mem_plan_set_wait_limit(h, 10 ** 6) == _lib.MEM_OK
+    finally:
+        lib.mem_plan_destroy(h)
