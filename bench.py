@@ -384,13 +384,13 @@ def workload_string(config_name, cfg, counts):
         int((counts * (counts - 1) // 2).sum()))
 
 
-def kernels_per_execute(outputs, avg_only, N):
+def kernels_per_execute(outputs, avg_only, N, counts=None, classes=None):
     """Kernels of this library one mem_plan_execute launches (cuFFT kernels excluded).
     N = 32, 64, 128 (shared-memory FFTs): lowpass_table, lowpass_fft, rot_const, rotate,
     spectrum_fft, qfix, pd_sums, pd_finalize, features, [inverse_fft + avg_store],
-    [inverse_fft + intensity], [contraction].  Other N (cuFFT transforms): lowpass_table,
-    gather_normalize, lowpass_apply, rot_const, rotate, qfix, pd_sums, pd_finalize, features,
-    [avg_store], [intensity], [contraction]."""
+    [inverse_fft + intensity], [contraction: one launch per size class that has PDs].  Other N
+    (cuFFT transforms): lowpass_table, gather_normalize, lowpass_apply, rot_const, rotate,
+    qfix, pd_sums, pd_finalize, features, [avg_store], [intensity], [contraction]."""
     smem = N in (32, 64, 128) and os.environ.get('MEM_SMEM_FFT', '1') != '0'
     k = 9
     if 'img_avg' in outputs or 'img_avg_flip' in outputs:
@@ -400,7 +400,16 @@ def kernels_per_execute(outputs, avg_only, N):
     if 'img_all_intensity' in outputs:
         k += 1
     if 'D' in outputs and not avg_only:
-        k += 1
+        if counts is not None and classes:
+            used = set()
+            for n in counts:
+                for i, c in enumerate(classes):
+                    if n <= c['max_n'] or i == len(classes) - 1:
+                        used.add(i)
+                        break
+            k += len(used)
+        else:
+            k += 1
     return k
 
 
@@ -506,6 +515,7 @@ def run_gpu(args, rank, world):
         tuned = autotune.tune(params, dev, force=args.autotune == 'force')
         t_tune = time.time() - t0
     plan = Plan(params, counts, [g.psi_p for g in geoms], dev)
+    plan_classes = plan.contraction
     outputs = tuple(args.outputs.split(','))
     outs = plan.allocate_outputs(outputs)
     sidx_h = np.concatenate([g.stack_index for g in geoms])
@@ -618,7 +628,86 @@ def run_gpu(args, rank, world):
                 graph=graph_used, l2_flush=flush, forms=forms, tuned=tuned, t_tune=t_tune,
                 phases=phases, clocks=clk.summary(), t_gen=t_gen, e2e=e2e, ds=ds, cfg=cfg, dm=dm,
                 nlsa=nlsa,
-                kernels=kernels_per_execute(outputs, False, cfg.N), outputs=outputs)
+                kernels=kernels_per_execute(outputs, False, cfg.N, counts, plan_classes),
+                outputs=outputs)
+
+
+def run_gpu_batched(args, rank, world, budget_frac=0.8):
+    """A workload larger than one device (config5: 1500 PDs of 250 px, about 2.2 million
+    images): the PDs are admitted into batches by the device-memory budget
+    (pipeline.admit_batches, as GetDistancesS2.run_jobs does), each batch's images are rendered
+    on the device outside the timed region, and each batch is timed like a single-plan
+    workload (graph replay, W warm-up and K timed steps); a step of the workload is the sum of
+    its batches' steps."""
+    import dataclasses
+    import torch
+    from manifoldem_python_gb300.geometry import pd_geometry
+    from manifoldem_python_gb300.pipeline import Plan, StageParams, admit_batches
+    from manifoldem_python_gb300.synthetic import CONFIGS, make_geometry, render_pds
+    dev = torch.device('cuda', int(os.environ.get('LOCAL_RANK', 0)))
+    torch.cuda.set_device(dev)
+    cfg = CONFIGS[args.config]
+    if args.n_pd:
+        cfg = dataclasses.replace(cfg, n_pd=args.n_pd)
+    cfg = dataclasses.replace(cfg, seed=cfg.seed + 1000 * rank)
+    t0 = time.time()
+    geo = make_geometry(cfg)
+    counts = [int(len(ind)) for ind in geo['CG']]
+    params = StageParams(N=cfg.N, pix_size=cfg.pix, Cs=cfg.cs, EkV=cfg.kv,
+                         AmpContrast=cfg.ampc, precision=args.precision)
+    tuned, t_tune = None, 0.0
+    if args.autotune and params.precision == 'bf16x3':
+        from manifoldem_python_gb300 import autotune
+        t1 = time.time()
+        tuned = autotune.tune(params, dev, force=args.autotune == 'force')
+        t_tune = time.time() - t1
+    torch.cuda.empty_cache()
+    free, _ = torch.cuda.mem_get_info(dev)
+    batches = admit_batches(counts, params, int(free * budget_frac))
+    outputs = tuple(args.outputs.split(','))
+    total_ms, pairs, n_images, n_kern, t_render = 0.0, 0, 0, 0, 0.0
+    phases, per_batch = {}, []
+    with ClockSampler(dev.index) as clk:
+        for b in batches:
+            t1 = time.time()
+            ds = render_pds(cfg, geo, b, device=dev)
+            torch.cuda.synchronize(dev)
+            t_render += time.time() - t1
+            geoms = [pd_geometry(np.asarray(ind), ds.q[:, ind], ds.nStot) for ind in ds.CG]
+            bc = [int(len(ind)) for ind in ds.CG]
+            plan = Plan(params, bc, [g.psi_p for g in geoms], dev)
+            outs = plan.allocate_outputs(outputs)
+            t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+            sidx = t(np.concatenate([g.stack_index for g in geoms]))
+            flip = t(np.concatenate([g.flip for g in geoms]))
+            psi = t(np.concatenate([g.psi_rad for g in geoms]))
+            dfd = t(np.concatenate([ds.df[ind] for ind in ds.CG]).astype(np.float64))
+            ms, ph, graph = time_form(plan, ds.stack, sidx, flip, psi, dfd, outs, args, world,
+                                      dev, False)
+            total_ms += ms
+            pairs += plan.n_pairs
+            n_images += plan.n_images
+            n_kern += kernels_per_execute(outputs, False, cfg.N, bc, plan.contraction)
+            for k, v in ph.items():
+                phases[k] = phases.get(k, 0.0) + v
+            per_batch.append(dict(pds=len(b), images=plan.n_images, pairs=plan.n_pairs,
+                                  ms=ms, contraction_ms=ph['contraction']))
+            del graph, plan, outs, ds, sidx, flip, psi, dfd
+            torch.cuda.synchronize(dev)
+            torch.cuda.empty_cache()
+    forms = {args.precision: dict(ms_per_step=total_ms, contraction_ms=phases['contraction'],
+                                  pairs_per_s=pairs / (total_ms * 1e-3), phases_ms=phases)}
+    # one PD of the workload, rendered alone, for the precision report
+    small = int(np.argmin(counts))
+    ds = render_pds(cfg, geo, [small], device=dev)
+    return dict(ms=total_ms, pairs=pairs, n_images=n_images, counts=counts, graph=args.graph,
+                l2_flush=False, forms=forms, tuned=tuned, t_tune=t_tune, phases=phases,
+                clocks=clk.summary(), t_gen=time.time() - t0, e2e=None, ds=ds, cfg=cfg,
+                dm=None, nlsa=None, kernels=n_kern, outputs=outputs,
+                precision_counts=[counts[small]],
+                batches=dict(count=len(batches), budget_bytes=int(free * budget_frac),
+                             render_s=t_render, per_batch=per_batch),
+                stack_gb=sum(counts) * cfg.N * cfg.N * 4 / 1e9)
 
 
 def roofline(r, args):
@@ -758,6 +847,64 @@ def fullsize_precision(ds, cfg, dev, pd=0):
     return rep
 
 
+def dropin_io_report(ds, cfg, n_pd=20, workdir=None):
+    """The drop-in driver's real end-to-end cost (GetDistancesS2.run_jobs, reference
+    GetDistancesS2.py:94-120 with myio.fout1, myio.py:38-51): the first n_pd PDs of the
+    workload from a SPIDER stack file on disk to one 19-key pickle and resume marker per PD, in
+    three modes -- float64 per-image arrays written in line (the reference's format and order),
+    float64 with four writer threads overlapping the GPU batches, and the float32 opt-in with
+    four writers.  Reports seconds, bytes written and GB/s to disk beside the GPU stage time."""
+    import shutil
+    import tempfile
+    from manifoldem_python_gb300 import GetDistancesS2 as G
+    from manifoldem_python_gb300 import p as mp
+    base = tempfile.mkdtemp(prefix='dropin_io_', dir=workdir)
+    try:
+        pds = list(range(min(n_pd, len(ds.CG))))
+        # a stack file holding only these PDs' particles, job indices remapped to it (conjugate
+        # views stay above the new particle count)
+        npart = ds.num_part
+        phys = [np.where(ds.CG[i] >= npart, ds.CG[i] - npart, ds.CG[i]) for i in pds]
+        keep = np.unique(np.concatenate(phys))
+        remap = np.full(npart, -1, dtype=np.int64)
+        remap[keep] = np.arange(keep.size)
+        inds = [remap[ph] + np.where(ds.CG[i] >= npart, keep.size, 0)
+                for i, ph in zip(pds, phys)]
+        stack_file = os.path.join(base, 'stack.bin')
+        sel = ds.stack[keep] if hasattr(ds.stack, 'cpu') else np.asarray(ds.stack)[keep]
+        host = sel.cpu().numpy() if hasattr(sel, 'cpu') else np.asarray(sel)
+        host.astype(np.float32).tofile(stack_file)
+        nStot = 2 * int(keep.size)
+        mp.init()
+        mp.nPix, mp.pix_size, mp.Cs, mp.EkV, mp.AmpContrast = cfg.N, cfg.pix, cfg.cs, cfg.kv, \
+            cfg.ampc
+        options = dict(verbose=False, avgOnly=False, visual=False, parallel=False,
+                       relion_data=False, thres=6000)
+        jobs_of = lambda d: [[ind, ds.q[:, ds.CG[i]], ds.df[ds.CG[i]],
+                              os.path.join(d, 'IMGs_prD_%d' % i), i] for i, ind in zip(pds, inds)]
+        n_img = int(sum(len(ds.CG[i]) for i in pds))
+        out = dict(pds=len(pds), images=n_img, N=cfg.N)
+        for name, dtype, writers in (('f64_inline', np.float64, 0), ('f64_4writers', np.float64, 4),
+                                     ('f32_4writers', np.float32, 4)):
+            d = os.path.join(base, name)
+            mp.dist_prog = os.path.join(d, 'progress')
+            os.makedirs(mp.dist_prog)
+            t0 = time.perf_counter()
+            G.run_jobs(jobs_of(d), stack_file, nStot, options, writers=writers,
+                       image_dtype=dtype, precision='bf16x3')
+            sec = time.perf_counter() - t0
+            nbytes = sum(os.path.getsize(os.path.join(d, f)) for f in os.listdir(d)
+                         if f.startswith('IMGs_prD_'))
+            out[name] = dict(seconds=sec, bytes=nbytes, gb_per_s=nbytes / sec / 1e9)
+            shutil.rmtree(d)
+        out['method'] = ('GetDistancesS2.run_jobs on the PDs, stack read from a raw file, '
+                         'pickles to local disk; f32 = the image_dtype opt-in (CTF, imgAll, '
+                         'imgAllFlip kept in the float32 the GPU computes them in)')
+        return out
+    finally:
+        shutil.rmtree(base, ignore_errors=True)
+
+
 def cpu_baseline(args, ds, counts, cfg, steps=1, budget_s=20.0):
     cores = os.cpu_count() or 1
     mic = dict(N=cfg.N, pix_size=cfg.pix, Cs=cfg.cs, EkV=cfg.kv, AmpContrast=cfg.ampc)
@@ -784,6 +931,41 @@ def cpu_baseline(args, ds, counts, cfg, steps=1, budget_s=20.0):
               % (len(pick), what, ns, args.config, len(counts), fit['a'], fit['b'], walls[-1]))
     return dict(value=float(np.median(vals)), unit='pairs/s', cores=cores, kind='port',
                 sample=sample), walls
+
+
+def cpu_port_rate(args, cfg, counts, steps, warmup=0):
+    """The FP64 CPU port of the reference (oracle/) on the host cores: PDs at evenly spaced
+    size quantiles (at most --cpu-max-n images; sub-PDs of the largest PD when fewer than four
+    qualify), rendered on the CPU, one process per core; pairs/s extrapolated to the whole
+    workload by t(n) = a n + b n^2.  Returns (median pairs/s, wall seconds per step, cores,
+    description of the sample)."""
+    from manifoldem_python_gb300.synthetic import make_dataset
+    cores = os.cpu_count() or 1
+    pick = choose_sample(np.asarray(counts), cores, max_n=args.cpu_max_n)
+    sizes = None
+    if len(pick) < 4:
+        big = int(np.argmax(counts))
+        top = min(int(counts[big]), args.cpu_max_n)
+        sizes = sorted(set(int(x) for x in np.linspace(max(20, top // 6), top, min(cores, 6))))
+        pick = [big] * len(sizes)
+    uniq = sorted(set(pick))
+    ds = make_dataset(cfg, device='cpu', pd_select=uniq)
+    mic = dict(N=cfg.N, pix_size=cfg.pix, Cs=cfg.cs, EkV=cfg.kv, AmpContrast=cfg.ampc)
+    tasks = cpu_sample_tasks(ds, [uniq.index(p) for p in pick], mic, sizes)
+    for _ in range(warmup):
+        run_cpu_tasks(tasks[:1], 1)
+    vals, walls = [], []
+    for _ in range(steps):
+        res, wall = run_cpu_tasks(tasks, cores)
+        v, fit = extrapolate_pairs_per_s(res, wall, counts, cores)
+        vals.append(v)
+        walls.append(wall)
+    ns = sizes if sizes is not None else sorted(int(counts[p]) for p in pick)
+    sample = ('%d %s (n=%s) of the %s workload per step, one per core, FP64 CPU port of '
+              'the reference (oracle/); pairs/s extrapolated to all %d PDs by '
+              't(n)=a n + b n^2' % (len(pick), 'sub-PDs' if sizes else 'PDs at size quantiles',
+                                    ns, args.config, len(counts)))
+    return float(np.median(vals)), walls, cores, sample
 
 
 def main():
@@ -824,6 +1006,11 @@ def main():
     ap.add_argument('--no-precision', action='store_true',
                     help='skip the FP64 / diffusion-map precision report of one sample PD')
     ap.add_argument('--cpu-max-n', type=int, default=900)
+    ap.add_argument('--dropin-io', type=int, default=0,
+                    help='time GetDistancesS2.run_jobs with pickle writes on this many PDs')
+    ap.add_argument('--batched', action='store_true',
+                    help='admit the PDs into device-memory batches rendered one at a time '
+                         '(default for config5, whose images do not fit on one device)')
     ap.add_argument('--fullsize-precision', action='store_true',
                     help='D of the whole first PD against a device FP64 contraction, with '
                          'near-duplicate and diffusion-map errors (default for config3)')
@@ -861,39 +1048,13 @@ def main():
     if args.impl == 'reference':
         if rank != 0:
             return
-        from manifoldem_python_gb300.synthetic import CONFIGS, make_dataset, particle_counts
+        from manifoldem_python_gb300.synthetic import CONFIGS, particle_counts
         import dataclasses
         cfg = CONFIGS[args.config]
         if args.n_pd:
             cfg = dataclasses.replace(cfg, n_pd=args.n_pd)
         counts = particle_counts(cfg)[:cfg.n_pd]
-        cores = os.cpu_count() or 1
-        pick = choose_sample(counts, cores, max_n=args.cpu_max_n)
-        sizes = None
-        if len(pick) < 4:
-            big = int(np.argmax(counts))
-            top = min(int(counts[big]), args.cpu_max_n)
-            sizes = sorted(set(int(x) for x in np.linspace(max(20, top // 6), top,
-                                                            min(cores, 6))))
-            pick = [big] * len(sizes)
-        uniq = sorted(set(pick))
-        ds = make_dataset(cfg, device='cpu', pd_select=uniq)
-        mic = dict(N=cfg.N, pix_size=cfg.pix, Cs=cfg.cs, EkV=cfg.kv, AmpContrast=cfg.ampc)
-        tasks = cpu_sample_tasks(ds, [uniq.index(p) for p in pick], mic, sizes)
-        for _ in range(args.warmup):
-            run_cpu_tasks(tasks[:1], 1)
-        vals, walls = [], []
-        for _ in range(args.steps):
-            res, wall = run_cpu_tasks(tasks, cores)
-            v, fit = extrapolate_pairs_per_s(res, wall, counts, cores)
-            vals.append(v)
-            walls.append(wall)
-        v = float(np.median(vals))
-        ns = sizes if sizes is not None else sorted(int(counts[p]) for p in pick)
-        sample = ('%d %s (n=%s) of the %s workload per step, one per core, FP64 CPU port of '
-                  'the reference (oracle/); pairs/s extrapolated to all %d PDs by '
-                  't(n)=a n + b n^2' % (len(pick), 'sub-PDs' if sizes else 'PDs at size quantiles',
-                                        ns, args.config, len(counts)))
+        v, walls, cores, sample = cpu_port_rate(args, cfg, counts, args.steps, args.warmup)
         line = dict(metric=metric, value=v, unit='pairs/s', n_gpus=args.gpus, steps=args.steps,
                     warmup=args.warmup, ms_per_step=float(np.median(walls)) * 1000,
                     higher_is_better=True, scaling='weak', vs_baseline=None, dtype='f64',
@@ -909,7 +1070,8 @@ def main():
     import torch
     if world > 1:
         torch.distributed.init_process_group('nccl')
-    r = run_gpu(args, rank, world)
+    batched = args.batched or args.config == 'config5'
+    r = run_gpu_batched(args, rank, world) if batched else run_gpu(args, rank, world)
     pairs_total = r['pairs'] * world
     value = pairs_total / (r['ms'] * 1e-3)
     if rank != 0:
@@ -927,7 +1089,7 @@ def main():
                     precision=args.precision, outputs=list(r['outputs']),
                     l2=('L2 flushed before every timed step (%.2f GB image stack)'
                         if r['l2_flush'] else 'inputs larger than L2 (%.1f GB image stack)') % (
-                        r['ds'].stack.numel() * 4 / 1e9),
+                        r.get('stack_gb', r['ds'].stack.numel() * 4 / 1e9)),
                     parallelism='PD-sharded, one process per GPU' if world > 1 else 'single GPU',
                     cuda_graph=r['graph']),
         roofline=dict(bound=rl['bound'], achieved=rl['achieved'], peak=rl['peak'],
@@ -942,6 +1104,25 @@ def main():
         line['e2e'] = dict(value=pairs_total / (e['ms'] * 1e-3), unit='pairs/s',
                            h2d_bytes_per_step=e['h2d'], d2h_bytes_per_step=e['d2h'],
                            ms_per_step=e['ms'], pinned=e['pinned'], mode=e['mode'])
+    if r['phases'].get('contraction'):
+        from manifoldem_python_gb300.pipeline import feature_columns
+        peaks = load_peaks()
+        Kalg = 4 * cfg.N * (cfg.N // 2 + 1)
+        c_ms = r['phases']['contraction']
+        alg = 2.0 * Kalg * r['pairs'] / (c_ms * 1e-3) / 1e12
+        exe = 2.0 * 3 * feature_columns(cfg.N) * r['pairs'] / (c_ms * 1e-3) / 1e12
+        line['contraction'] = dict(
+            ms=c_ms, algorithmic_tflops=alg, frac_of_bf16_sustained=alg / peaks['bf16_sust'],
+            issued_tflops_needed_pairs=exe,
+            issued_frac_of_bf16_sustained=exe / peaks['bf16_sust'],
+            note='algorithmic: 2 K flop per unordered pair, K = 4 N (N/2+1) (the reference '
+                 'formulation); issued: three BF16 products over the Kf ring-feature columns '
+                 'per needed pair (tile padding and diagonal halves not counted)')
+    if r.get('batches'):
+        line['config']['batches'] = ('%d HBM-admitted PD batches, images rendered on the device '
+                                     'outside the timed region; a step is the sum of the '
+                                     "batches' steps" % r['batches']['count'])
+        line['batches'] = r['batches']
     if r.get('dm'):
         line['dm_embedding'] = r['dm']
     if r.get('nlsa'):
@@ -954,7 +1135,7 @@ def main():
     forms = r['forms']
     if not args.no_precision:
         for f in forms:
-            pr = precision_report(args, r['ds'], r['counts'], cfg, f)
+            pr = precision_report(args, r['ds'], r.get('precision_counts', r['counts']), cfg, f)
             forms[f]['D_err_vs_fp64_oracle'] = pr['max_rel_err_vs_fp64_oracle']
             forms[f]['D_err_vs_fp64_contraction'] = pr['max_rel_err_vs_fp64_contraction']
             forms[f]['dm_top8_subspace_angle_rad'] = pr['dm_top8_subspace_angle_rad']
@@ -969,9 +1150,16 @@ def main():
     if args.fullsize_precision or (args.config == 'config3' and not args.no_precision):
         import torch
         line['precision_fullsize'] = fullsize_precision(r['ds'], cfg, torch.device('cuda'))
+    if args.dropin_io:
+        line['dropin_io'] = dropin_io_report(r['ds'], cfg, n_pd=args.dropin_io)
     if not args.no_cpu_baseline:
-        cb, _ = cpu_baseline(args, r['ds'], r['counts'], cfg)
-        line['cpu_baseline'] = cb
+        if r.get('batches'):
+            v, _, cores, sample = cpu_port_rate(args, cfg, r['counts'], 1)
+            line['cpu_baseline'] = dict(value=v, unit='pairs/s', cores=cores, kind='port',
+                                        sample=sample)
+        else:
+            cb, _ = cpu_baseline(args, r['ds'], r['counts'], cfg)
+            line['cpu_baseline'] = cb
     print(json.dumps(line))
     if world > 1:
         torch.distributed.barrier()

@@ -144,6 +144,11 @@ typedef struct mem_contraction_config {
     int32_t tile_n;         /* D columns per tile: 128, or 256 (128 x 256 tiles: a quarter
                                fewer operand bytes per MMA, two 96 KB stages instead of three
                                64 KB ones); 0 means 128                                        */
+    int32_t tile_m;         /* D rows per tile: 128 (one SM), or 256 (a pair of SMs sharing
+                               one MMA stream, tcgen05.mma.cta_group::2: each SM loads 128 A
+                               rows and half of the 128 B rows, 48 KB per K chunk, four stages;
+                               needs tile_n 128); 0 means 128                                  */
+    int32_t reserved;       /* 0                                                               */
 } mem_contraction_config;
 
 /* Sets the plan's contraction schedule (HOST array of n_classes >= 1 entries, max_n

@@ -123,7 +123,7 @@ class MemInputs(ctypes.Structure):
 
 class MemContractionConfig(ctypes.Structure):
     _fields_ = [('max_n', c_int32), ('persistent', c_int32), ('accumulators', c_int32),
-                ('tile_n', c_int32)]
+                ('tile_n', c_int32), ('tile_m', c_int32), ('reserved', c_int32)]
 
 
 class MemOutputs(ctypes.Structure):

@@ -2,14 +2,16 @@
 
 The tensor-core contraction of D (include/manifoldem_gb300.h, ``mem_contraction_config``) runs
 the tiles of each size class of PDs in one launch with the class's schedule: tiles of 128 x 128
-or 128 x 256 entries of D (the wider tile reads a quarter fewer operand bytes per MMA but pads
-small PDs more and has two pipeline stages instead of three), one CTA per tile or one
-persistent CTA per SM walking its tiles, with two or four TMEM accumulators (how many
-accumulation groups the MMA issuer may run ahead of the epilogue, across tile boundaries).
-Which is fastest depends on the PD size (padding, tiles per PD, the tail of the last wave) and
-on the box size (K, the length of each tile's main loop), so the choice is measured: for each class a synthetic batch of PDs of the class's typical size
-is planned once per candidate schedule and its contraction phase timed with the library's phase
-events (median of a few executes), and the fastest schedule is kept.
+or 128 x 256 entries of D on one SM, or 256 x 128 on a pair of SMs sharing one MMA stream (the
+larger tiles read a quarter fewer operand bytes per MMA but pad small PDs more), one CTA per
+tile or one persistent CTA per SM walking its tiles, with two or four TMEM accumulators (how
+many accumulation groups the MMA issuer may run ahead of the epilogue, across tile
+boundaries).  Which is fastest depends on the PD size (padding, tiles per PD, the tail of the
+last wave) and on the box size (K, the length of each tile's main loop), so the choice is
+measured: for each class a synthetic batch of PDs of the class's typical size is planned once
+per candidate schedule and its contraction phase timed with the library's phase events (median
+of a few executes); the simplest schedule is kept unless another is clearly faster, and
+adjacent classes that chose the same schedule are merged into one launch.
 
 Results are cached in a JSON file keyed by GPU name, box size and contraction form
 (``MEM_AUTOTUNE_CACHE`` names the file; default ``autotune_cache.json`` beside this module);
@@ -35,9 +37,13 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 # is tuned on
 CLASS_MAX_N = (192, 640, 1536, 2 ** 31 - 1)
 CLASS_REP_N = (160, 400, 1000, 2500)
-# candidate schedules: (persistent, accumulators, tile width)
-CANDIDATES = ((0, 2, 128), (1, 2, 128), (1, 4, 128), (0, 2, 256), (1, 2, 256))
-TARGET_TILES = 456          # about three waves of 128 x 128 tiles on 152 SMs
+# candidate schedules, simplest first: (persistent, accumulators, tile width, tile height);
+# height 256 = a pair of SMs sharing one MMA stream
+CANDIDATES = ((0, 2, 128, 128), (1, 2, 128, 128), (1, 4, 128, 128), (0, 2, 256, 128),
+              (1, 2, 256, 128), (0, 2, 128, 256), (1, 2, 128, 256), (1, 4, 128, 256))
+TARGET_TILES = 1216         # about eight waves of 128 x 128 tiles on 152 SMs
+# a schedule later in CANDIDATES (more machinery) must beat the current choice by this fraction
+TIE_MARGIN = 0.03
 
 _lock = threading.Lock()
 
@@ -80,6 +86,8 @@ def to_c(classes: Sequence[dict]):
         arr[i].persistent = int(c['persistent'])
         arr[i].accumulators = int(c['accumulators'])
         arr[i].tile_n = int(c.get('tile_n', 128))
+        arr[i].tile_m = int(c.get('tile_m', 128))
+        arr[i].reserved = 0
     return arr
 
 
@@ -90,12 +98,13 @@ def _class_batch(rep_n: int) -> List[int]:
     return [rep_n] * n_pd
 
 
-def _time_schedule(params, counts, sched: Tuple[int, int, int], device, reps: int = 5) -> float:
+def _time_schedule(params, counts, sched: Tuple[int, int, int, int], device,
+                   reps: int = 5) -> float:
     """Median contraction-phase time (ms) of a plan of `counts` random PDs with one schedule."""
     import torch
     from .pipeline import Plan
     cfg = [dict(max_n=2 ** 31 - 1, persistent=sched[0], accumulators=sched[1],
-                tile_n=sched[2])]
+                tile_n=sched[2], tile_m=sched[3])]
     plan = Plan(params, counts, [0.0] * len(counts), device, contraction=cfg)
     n_img = plan.n_images
     g = torch.Generator(device=device).manual_seed(1)
@@ -140,13 +149,44 @@ def tune(params, device=None, force: bool = False) -> List[dict]:
     for max_n, rep_n in zip(CLASS_MAX_N, CLASS_REP_N):
         counts = _class_batch(rep_n)
         ms = {s: _time_schedule(p, counts, s, device) for s in CANDIDATES}
-        best = min(ms, key=ms.get)
+        best = pick(ms)
         classes.append(dict(max_n=int(max_n), persistent=best[0], accumulators=best[1],
-                            tile_n=best[2], rep_n=rep_n, pds=len(counts),
-                            ms={'%d,%d,%d' % s: round(v, 4) for s, v in ms.items()}))
+                            tile_n=best[2], tile_m=best[3], rep_n=rep_n, pds=len(counts),
+                            ms={'%d,%d,%d,%d' % s: round(v, 4) for s, v in ms.items()}))
         torch.cuda.empty_cache()
+    classes = merge_classes(classes)
     with _lock:
         d = _read_cache()
         d[cache_key(name, params.N, params.precision)] = dict(classes=classes)
         _write_cache(d)
     return classes
+
+
+def pick(ms: Dict[tuple, float]) -> tuple:
+    """The schedule of a class from its measured times: walking CANDIDATES in order (simplest
+    first), a later schedule replaces the current choice only when it is faster by more than
+    TIE_MARGIN."""
+    order = [c for c in CANDIDATES if c in ms]
+    best = order[0]
+    for cand in order[1:]:
+        if ms[cand] < ms[best] * (1.0 - TIE_MARGIN):
+            best = cand
+    return best
+
+
+def merge_classes(classes: List[dict]) -> List[dict]:
+    """Adjacent classes with the same schedule become one (one launch instead of two, one
+    tail instead of two); the merged class keeps the larger max_n and both measurements."""
+    key = lambda c: (c['persistent'], c['accumulators'], c.get('tile_n', 128),
+                     c.get('tile_m', 128))
+    out: List[dict] = []
+    for c in classes:
+        if out and key(out[-1]) == key(c):
+            prev = out[-1]
+            prev['max_n'] = c['max_n']
+            prev['merged'] = prev.get('merged', [dict(rep_n=prev.get('rep_n'),
+                                                      ms=prev.get('ms'))])
+            prev['merged'].append(dict(rep_n=c.get('rep_n'), ms=c.get('ms')))
+        else:
+            out.append(dict(c))
+    return out

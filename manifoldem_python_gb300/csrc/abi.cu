@@ -275,11 +275,13 @@ void wait_settings_from_env(long long* cycles, int* withhold) {
 }
 
 mem_contraction_config default_contraction() {
-    mem_contraction_config c{INT32_MAX, 0, 2, 128};
+    mem_contraction_config c{INT32_MAX, 0, 2, 128, 128, 0};
     if (const char* e = std::getenv("MEM_TC_PERSISTENT")) c.persistent = std::atoi(e) != 0;
     if (const char* e = std::getenv("MEM_TC_BUFS")) c.accumulators = std::atoi(e) == 4 ? 4 : 2;
     if (const char* e = std::getenv("MEM_TC_TILE_N")) c.tile_n = std::atoi(e) == 256 ? 256 : 128;
+    if (const char* e = std::getenv("MEM_TC_TILE_M")) c.tile_m = std::atoi(e) == 256 ? 256 : 128;
     if (c.tile_n == 256) c.accumulators = 2;
+    if (c.tile_m == 256) c.tile_n = 128;
     return c;
 }
 
@@ -291,7 +293,9 @@ int apply_contraction(mem_plan* P, int n_classes, const mem_contraction_config* 
         if (c.persistent != 0 && c.persistent != 1) return MEM_ERR_INVALID;
         if (c.accumulators != 2 && c.accumulators != 4) return MEM_ERR_INVALID;
         if (c.tile_n != 0 && c.tile_n != 128 && c.tile_n != 256) return MEM_ERR_INVALID;
+        if (c.tile_m != 0 && c.tile_m != 128 && c.tile_m != 256) return MEM_ERR_INVALID;
         if (c.tile_n == 256 && c.accumulators != 2) return MEM_ERR_INVALID;
+        if (c.tile_m == 256 && c.tile_n == 256) return MEM_ERR_INVALID;
     }
     auto cls = [&](int n) {
         for (int k = 0; k < n_classes - 1; ++k)
@@ -300,22 +304,24 @@ int apply_contraction(mem_plan* P, int n_classes, const mem_contraction_config* 
     };
     P->tc_classes.assign(classes, classes + n_classes);
     for (mem_contraction_config& c : P->tc_classes) {
-        // the compensated epilogue sums of 256-wide tiles would not fit the register file
+        // the compensated epilogue sums (a tuning option) exist in the one-SM 128 x 128 kernel
+        // only: the 256-wide tile's would not fit the register file
         if (c.tile_n != 256 || P->tc_kahan) c.tile_n = 128;
+        if (c.tile_m != 256 || P->tc_kahan) c.tile_m = 128;
     }
-    // the tiles of every class, class by class, PDs in plan order: 128-row blocks I and
-    // column blocks J of the class's width that meet the upper triangle (J >= 128 I / width)
+    // the tiles of every class, class by class, PDs in plan order: row blocks I and column
+    // blocks J of the class's tile shape that meet the upper triangle (J >= I bm / bn)
     P->tc_tiles.clear();
     P->tc_ranges.assign(n_classes, std::make_pair(0, 0));
     for (int k = 0; k < n_classes; ++k) {
-        const int bn = P->tc_classes[k].tile_n;
+        const int bn = P->tc_classes[k].tile_n, bm = P->tc_classes[k].tile_m;
         P->tc_ranges[k].first = (int)P->tc_tiles.size();
         for (int i = 0; i < P->n_pd; ++i) {
             const int n = P->pd[i].n;
             if (cls(n) != k) continue;
-            const int nb = (n + kRowBlock - 1) / kRowBlock, nj = (n + bn - 1) / bn;
+            const int nb = (n + bm - 1) / bm, nj = (n + bn - 1) / bn;
             for (int I = 0; I < nb; ++I)
-                for (int J = (I * kRowBlock) / bn; J < nj; ++J)
+                for (int J = (I * bm) / bn; J < nj; ++J)
                     P->tc_tiles.push_back(Tile{i, I, J, 0});
         }
         P->tc_ranges[k].second = (int)P->tc_tiles.size() - P->tc_ranges[k].first;

@@ -21,14 +21,14 @@
 // Every mbarrier wait is bounded: on expiry the CTA sets the status word's timeout bit, stops
 // issuing, waits (bounded) for its own TMA copies and MMAs, frees its TMEM and returns.
 #include <algorithm>
-#include <cuda.h>
 #include <type_traits>
-#include <cudaTypedefs.h>
 
-#include "mem_internal.cuh"
+#include "tcgen05.cuh"
 
 namespace mem {
 namespace {
+
+using namespace tc;
 
 constexpr int TC_M = 128, TC_BK = 64;
 constexpr int TC_EPI_WARPS = 8;
@@ -54,122 +54,6 @@ template <int BN>
 __host__ __device__ constexpr uint32_t idesc_f16() {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
            ((uint32_t)(TC_M >> 4) << 24);
-}
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
-                 : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
-                 "r"(bytes)
-                 : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}\n"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-// bounded wait (at most `limit` SM clock cycles); false if it expired or another role aborted
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
-                                          uint32_t* status, long long limit) {
-    if (mbar_try_wait(bar, parity)) return true;
-    const long long t0 = clock64();
-    while (!mbar_try_wait(bar, parity)) {
-        if (*abort_flag) return false;
-        if (clock64() - t0 > limit) {
-            *abort_flag = 1;
-            atomicOr(status, kStatusTimeout);
-            return false;
-        }
-    }
-    return true;
-}
-
-// bounded wait used while draining after an abort (no abort check)
-__device__ __forceinline__ void mbar_drain(uint64_t* bar, uint32_t parity, long long limit) {
-    const long long t0 = clock64();
-    while (!mbar_try_wait(bar, parity))
-        if (clock64() - t0 > limit) return;
-}
-
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar,
-                                            int x, int y) {
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-        " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
-        "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_u32(bar))
-        : "memory");
-}
-
-// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart
-__device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
-    uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
-    d |= (uint64_t)1 << 16;                  // leading byte offset (unused for swizzled K-major)
-    d |= (uint64_t)(1024 >> 4) << 32;        // stride byte offset
-    d |= (uint64_t)1 << 46;                  // descriptor version
-    d |= (uint64_t)2 << 61;                  // SWIZZLE_128B
-    return d;
-}
-
-__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
-                                          uint32_t idesc, uint32_t accumulate) {
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "setp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
-        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
-        : "memory");
-}
-
-__device__ __forceinline__ void umma_commit(uint64_t* bar) {
-    asm volatile(
-        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-            smem_u32(bar))
-        : "memory");
-}
-
-__device__ __forceinline__ void tc_fence_before() {
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-}
-__device__ __forceinline__ void tc_fence_after() {
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-}
-
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
-        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
-          "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
-          "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
-          "=r"(r[31])
-        : "r"(taddr)
-        : "memory");
-}
-
-__device__ __forceinline__ void tmem_ld_wait() {
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
 constexpr int TC_MAX_BUFS = 4;
@@ -440,31 +324,268 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gemm_tc_kernel(
     }
 }
 
-PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    if (!fn) {
-        void* p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
-                                             cudaEnableDefault, &q) == cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
-    }
-    return fn;
-}
+// ---- the CTA-pair form: 256 x 128 tiles on two SMs (cta_group::2) --------------------------
+// A cluster of two CTAs on two SMs computes a 256 x 128 tile with one MMA stream: the even
+// CTA issues tcgen05.mma.cta_group::2 (M = 256, N = 128); each CTA holds 128 rows of A and 64
+// of the 128 B rows of every stage in its own shared memory, and 128 accumulator rows in its
+// own tensor memory.  Per SM a 64-wide K chunk moves 48 KB (A 32 KB, half of B 16 KB) instead
+// of the 64 KB of a 128 x 128 tile on one SM, and four stages fit in shared memory.
+//   loads:  both CTAs' TMA copies count on the even CTA's full barrier (the even CTA arms it
+//           with both CTAs' bytes);
+//   MMA:    one thread of the even CTA; its commits arrive on the stage's empty barrier and
+//           the accumulator's full barrier of both CTAs (multicast);
+//   epilogue: each CTA drains its own tensor memory and arrives on the even CTA's
+//           accumulator-empty barrier (16 arrivals per group).
+// Waits are bounded as in the one-SM kernel.  After an abort the even CTA waits (bounded) for
+// the stages it armed; the odd CTA, whose copies count on the even CTA's barriers, waits a
+// bounded time far longer than a copy takes before both CTAs meet at the final cluster barrier.
+constexpr int TP_STAGES = 4;
+constexpr int TP_OPB_B = 64 * TC_BK * 2;                      // one 64-row box: 8 KB
+constexpr int TP_STAGE_BYTES = 2 * TC_OPB + 2 * TP_OPB_B;      // 48 KB per CTA
+constexpr size_t TP_SMEM = (size_t)TP_STAGES * TP_STAGE_BYTES + 1024 + 512;
 
-int make_map(CUtensorMap* map, const void* base, int64_t Kf, int64_t rows) {
-    auto enc = get_encode();
-    if (!enc) return MEM_ERR_CUDA;
-    cuuint64_t dims[2] = {(cuuint64_t)Kf, (cuuint64_t)rows};
-    cuuint64_t strides[1] = {(cuuint64_t)(Kf * 2)};
-    cuuint32_t box[2] = {(cuuint32_t)TC_BK, (cuuint32_t)TC_M};
-    cuuint32_t estr[2] = {1, 1};
-    CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims,
-                     strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                     CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    return r == CUDA_SUCCESS ? MEM_OK : MEM_ERR_CUDA;
+struct TpShared {
+    uint64_t full[TP_STAGES];
+    uint64_t empty[TP_STAGES];
+    uint64_t acc_full[TC_MAX_BUFS];
+    uint64_t acc_empty[TC_MAX_BUFS];
+    uint64_t mma_done;
+    uint32_t tmem_base;
+    int abort_flag;
+};
+
+template <bool LOLO, int NBUF>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(TC_THREADS, 1) gemm_tc_pair_kernel(
+        const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CUtensorMap map_lo,
+        const __grid_constant__ CUtensorMap mapb_hi, const __grid_constant__ CUtensorMap mapb_lo,
+        const double* __restrict__ pair_norm, const uint32_t* __restrict__ scale_bits,
+        const Tile* __restrict__ tiles, const PdDev* __restrict__ pds, double* __restrict__ D,
+        uint32_t* __restrict__ status, const int4* __restrict__ chunks, int nchunks,
+        int group_chunks, long long wait_limit, int withhold, int tile_begin, int tile_count) {
+    static_assert(NBUF == 2 || NBUF == 4, "two or four TMEM accumulators");
+    constexpr int BN = 128, EC = 64;
+    constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                               ((uint32_t)(256 >> 4) << 24);
+    constexpr uint32_t IDESC_NEG = IDESC | (1u << 14);
+    constexpr uint32_t TMEM_COLS = NBUF * BN;
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    TpShared* sh = (TpShared*)(smem + TP_STAGES * TP_STAGE_BYTES);
+    volatile int* abort_flag = &sh->abort_flag;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t rank = cluster_ctarank();
+    const bool even = rank == 0;
+    const int pair = (int)(blockIdx.x >> 1), npairs = (int)(gridDim.x >> 1);
+    const int my_tiles = pair < tile_count ? (tile_count - pair + npairs - 1) / npairs : 0;
+    auto tile_of = [&](int lt) { return tiles[tile_begin + pair + lt * npairs]; };
+    const int gsize = (group_chunks > 0 && group_chunks < nchunks) ? group_chunks : nchunks;
+    const int ngroups = (nchunks + gsize - 1) / gsize;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < TP_STAGES; ++s) {
+            mbar_init(&sh->full[s], 1);
+            mbar_init(&sh->empty[s], 1);
+        }
+        for (int b = 0; b < NBUF; ++b) {
+            mbar_init(&sh->acc_full[b], 1);
+            mbar_init(&sh->acc_empty[b], 2 * TC_EPI_WARPS);
+        }
+        mbar_init(&sh->mma_done, 1);
+        sh->abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == TC_EPI_WARPS + 1) {
+        asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(&sh->tmem_base)),
+                     "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    cluster_sync();              // both CTAs' barriers and tensor memory are ready
+    tc_fence_after();
+    const uint32_t tmem = sh->tmem_base;
+    // the even CTA's full and accumulator-empty barriers, as cluster addresses
+    const uint32_t full_even = map_to_cta(smem_u32(&sh->full[0]), 0);
+    const uint32_t acc_empty_even = map_to_cta(smem_u32(&sh->acc_empty[0]), 0);
+
+    if (warp == TC_EPI_WARPS) {
+        // ---------------------------------------------------------------- TMA producer
+        if (lane == 0) {
+            asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&map_hi) : "memory");
+            asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&map_lo) : "memory");
+            asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&mapb_hi) : "memory");
+            asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&mapb_lo) : "memory");
+            long long gc = 0, withheld = -1;
+            bool stop = false;
+            for (int lt = 0; lt < my_tiles && !stop; ++lt) {
+                const Tile t = tile_of(lt);
+                const PdDev pd = pds[t.pd];
+                const int rowA = (int)(pd.row_off + (int64_t)t.I * 256 + rank * 128);
+                const int rowB = (int)(pd.row_off + (int64_t)t.J * BN + rank * 64);
+                for (int c = 0; c < nchunks; ++c, ++gc) {
+                    const int st = (int)(gc % TP_STAGES);
+                    const uint32_t ph = (uint32_t)(gc / TP_STAGES) & 1u;
+                    if (gc >= TP_STAGES &&
+                        !mbar_wait(&sh->empty[st], ph ^ 1u, abort_flag, status, wait_limit)) {
+                        stop = true;
+                        break;
+                    }
+                    if (lt == 0 && c == withhold) {      // test of the timeout path
+                        withheld = gc;
+                        continue;
+                    }
+                    const int4 ch = chunks[c];
+                    uint8_t* sb = smem + st * TP_STAGE_BYTES;
+                    if (even) mbar_expect_tx(&sh->full[st], 2 * TP_STAGE_BYTES);
+                    const uint32_t bar = full_even + 8u * (uint32_t)st;
+                    tma_load_2d_pair(sb, &map_hi, bar, ch.x, rowA);
+                    tma_load_2d_pair(sb + TC_OPB, &map_lo, bar, ch.x, rowA);
+                    tma_load_2d_pair(sb + 2 * TC_OPB, &mapb_hi, bar, ch.y, rowB);
+                    tma_load_2d_pair(sb + 2 * TC_OPB + TP_OPB_B, &mapb_lo, bar, ch.y, rowB);
+                }
+            }
+            if (*abort_flag) {
+                if (even) {      // the stages this CTA armed: both CTAs' copies have landed
+                    for (long long c = (gc > TP_STAGES ? gc - TP_STAGES : 0); c < gc; ++c)
+                        if (c != withheld)
+                            mbar_drain(&sh->full[c % TP_STAGES],
+                                       (uint32_t)(c / TP_STAGES) & 1u, wait_limit);
+                } else {         // copies count on the even CTA's barriers: a bounded pause
+                    const long long t0 = clock64();
+                    const long long pause = wait_limit < (1ll << 22) ? wait_limit : (1ll << 22);
+                    while (clock64() - t0 < pause) __nanosleep(1000);
+                }
+            }
+        }
+    } else if (warp == TC_EPI_WARPS + 1) {
+        // ---------------------------------------------------------------- MMA issuer
+        if (lane == 0 && even) {
+            bool issued_any = false, stop = false;
+            long long gc = 0, gg = 0;
+            for (int lt = 0; lt < my_tiles && !stop; ++lt) {
+                int4 ch_next = chunks[0];
+                for (int c = 0; c < nchunks; ++c, ++gc) {
+                    const int4 ch = ch_next;
+                    if (c + 1 < nchunks) ch_next = chunks[c + 1];
+                    const int st = (int)(gc % TP_STAGES);
+                    const uint32_t ph = (uint32_t)(gc / TP_STAGES) & 1u;
+                    const int b = (int)(gg % NBUF);
+                    const long long use = gg / NBUF;
+                    const bool first = (c % gsize) == 0;
+                    const bool last = ((c % gsize) == gsize - 1) || c == nchunks - 1;
+                    if (first && use >= 1 &&
+                        !mbar_wait(&sh->acc_empty[b], (uint32_t)((use - 1) & 1), abort_flag,
+                                   status, wait_limit)) {
+                        stop = true;
+                        break;
+                    }
+                    if (!mbar_wait(&sh->full[st], ph, abort_flag, status, wait_limit)) {
+                        stop = true;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t idesc = ch.z != 0 ? IDESC_NEG : IDESC;
+                    const uint32_t d = tmem + (uint32_t)(b * BN);
+                    const uint32_t sa = smem_u32(smem + st * TP_STAGE_BYTES);
+                    auto mma_chunk = [&](auto four) {
+#pragma unroll
+                        for (int k = 0; k < TC_BK / 16; ++k) {
+                            const uint64_t ahi = sdesc_sw128(sa + k * 32);
+                            const uint64_t alo = sdesc_sw128(sa + TC_OPB + k * 32);
+                            const uint64_t bhi = sdesc_sw128(sa + 2 * TC_OPB + k * 32);
+                            const uint64_t blo = sdesc_sw128(sa + 2 * TC_OPB + TP_OPB_B + k * 32);
+                            umma_bf16_pair(d, ahi, bhi, idesc, (first && k == 0) ? 0u : 1u);
+                            umma_bf16_pair(d, ahi, blo, idesc, 1u);
+                            umma_bf16_pair(d, alo, bhi, idesc, 1u);
+                            if (decltype(four)::value) umma_bf16_pair(d, alo, blo, idesc, 1u);
+                        }
+                    };
+                    if (LOLO || ch.w != 0)
+                        mma_chunk(std::true_type{});
+                    else
+                        mma_chunk(std::false_type{});
+                    issued_any = true;
+                    umma_commit_pair(&sh->empty[st], (uint16_t)3);
+                    if (last) {
+                        umma_commit_pair(&sh->acc_full[b], (uint16_t)3);
+                        ++gg;
+                    }
+                }
+            }
+            if (*abort_flag && issued_any) {   // wait for the MMAs in flight
+                umma_commit_pair(&sh->mma_done, (uint16_t)1);
+                mbar_drain(&sh->mma_done, 0, wait_limit);
+            }
+        }
+    } else {
+        // ---------------------------------------------------------------- epilogue
+        const int q = warp & 3, h = warp >> 2;
+        const int row = q * 32 + lane;
+        bool ok = true;
+        long long gg = 0;
+        for (int lt = 0; lt < my_tiles && ok; ++lt) {
+            const Tile t = tile_of(lt);
+            float acc[EC];
+#pragma unroll
+            for (int j = 0; j < EC; ++j) acc[j] = 0.f;
+            for (int g = 0; g < ngroups; ++g, ++gg) {
+                const int b = (int)(gg % NBUF);
+                const long long use = gg / NBUF;
+                ok = mbar_wait(&sh->acc_full[b], (uint32_t)(use & 1), abort_flag, status,
+                               wait_limit);
+                __syncwarp();
+                ok = __all_sync(0xffffffffu, ok);
+                if (!ok) break;
+                tc_fence_after();
+                const uint32_t taddr =
+                    tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN + h * EC);
+#pragma unroll
+                for (int half = 0; half < EC / 32; ++half) {
+                    uint32_t r[32];
+                    tmem_ld32(taddr + half * 32, r);
+                    tmem_ld_wait();
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) acc[half * 32 + j] += __uint_as_float(r[j]);
+                }
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive_cluster(acc_empty_even + 8u * (uint32_t)b);
+            }
+            if (!ok || *abort_flag) break;
+            const PdDev pd = pds[t.pd];
+            const double sc = (double)feature_scale_from_bits(scale_bits[t.pd]);
+            const double inv_sc2 = 1.0 / (sc * sc);
+            const int n = pd.n;
+            const int gi = t.I * 256 + (int)rank * 128 + row;
+            double* Dp = D + pd.d_off;
+            const double* an = pair_norm + pd.img_off;
+            if (gi < n) {
+                const double ai = an[gi];
+                const int j0 = t.J * BN + h * EC;
+#pragma unroll
+                for (int j = 0; j < EC; ++j) {
+                    const int gj = j0 + j;
+                    if (gj >= n || gj < gi) continue;
+                    if (gj == gi) {
+                        Dp[(int64_t)gi * n + gi] = 0.0;
+                        continue;
+                    }
+                    const double v = ai + an[gj] + (double)acc[j] * inv_sc2;
+                    Dp[(int64_t)gi * n + gj] = v;
+                    Dp[(int64_t)gj * n + gi] = v;
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    cluster_sync();              // the pair's MMAs, copies and remote arrivals are done
+    if (warp == TC_EPI_WARPS + 1) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                     "r"(TMEM_COLS)
+                     : "memory");
+    }
 }
 
 }  // namespace
@@ -479,16 +600,47 @@ int gemm_split_bf16(const mem_plan& P, const void* feat_hi, const void* feat_lo,
     if (P.Kf % TC_BK != 0 || P.n_rows % TC_M != 0 || (int64_t)P.n_chunks * TC_BK != P.Kf)
         return MEM_ERR_INVALID;
     CUtensorMap mhi, mlo;
-    int st = make_map(&mhi, feat_hi, P.Kf, P.n_rows);
+    int st = tc::make_map(&mhi, feat_hi, P.Kf, P.n_rows);
     if (st != MEM_OK) return st;
-    st = make_map(&mlo, feat_lo, P.Kf, P.n_rows);
+    st = tc::make_map(&mlo, feat_lo, P.Kf, P.n_rows);
     if (st != MEM_OK) return st;
     const int sms = P.num_sms > 0 ? P.num_sms : 1;
+    CUtensorMap bhi, blo;                // 64-row boxes: the CTA pairs' halves of B
+    bool have_b64 = false;
     // one launch per size class of the plan's contraction configuration (tiles sorted by class)
     for (size_t k = 0; k < P.tc_ranges.size(); ++k) {
         const int begin = P.tc_ranges[k].first, count = P.tc_ranges[k].second;
         if (count <= 0) continue;
         const mem_contraction_config& cfg = P.tc_classes[k];
+        if (cfg.tile_m == 256) {
+            if (!have_b64) {
+                st = tc::make_map(&bhi, feat_hi, P.Kf, P.n_rows, 64);
+                if (st != MEM_OK) return st;
+                st = tc::make_map(&blo, feat_lo, P.Kf, P.n_rows, 64);
+                if (st != MEM_OK) return st;
+                have_b64 = true;
+            }
+            const unsigned pgrid =
+                2u * (unsigned)(cfg.persistent ? std::min(count, std::max(1, sms / 2)) : count);
+#define MEM_TP_LAUNCH(LOLO, NB)                                                                \
+    do {                                                                                       \
+        MEM_CUDA_TRY(cudaFuncSetAttribute(gemm_tc_pair_kernel<LOLO, NB>,                       \
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize,         \
+                                          (int)TP_SMEM));                                      \
+        gemm_tc_pair_kernel<LOLO, NB><<<pgrid, TC_THREADS, TP_SMEM, s>>>(                      \
+            mhi, mlo, bhi, blo, pair_norm, scale_bits, tiles, pds, D, status, chunks,          \
+            P.n_chunks, P.tc_group_chunks, P.wait_cycles, P.test_withhold_chunk, begin,        \
+            count);                                                                            \
+    } while (0)
+            if (P.tc_lolo) {
+                if (cfg.accumulators == 4) MEM_TP_LAUNCH(true, 4); else MEM_TP_LAUNCH(true, 2);
+            } else {
+                if (cfg.accumulators == 4) MEM_TP_LAUNCH(false, 4); else MEM_TP_LAUNCH(false, 2);
+            }
+#undef MEM_TP_LAUNCH
+            MEM_LAUNCH_CHECK();
+            continue;
+        }
         const unsigned grid = cfg.persistent ? (unsigned)std::min(count, sms) : (unsigned)count;
 #define MEM_TC_LAUNCH(KAHAN, LOLO, NB, BN)                                                     \
     do {                                                                                       \

@@ -152,6 +152,7 @@ void one_pd_tables(mem_plan& P, const mem_params& prm, int n) {
     // the tile table is written by noalloc_tables_kernel: 128-wide tiles
     mem_contraction_config dc = default_contraction();
     dc.tile_n = 128;
+    dc.tile_m = 128;
     apply_contraction(&P, 1, &dc);
     for (int64_t b = 0; b < n; b += kSumChunk)
         P.items.push_back(SumItem{0, 0, b, std::min<int64_t>(n, b + kSumChunk)});

@@ -99,13 +99,16 @@ def test_contraction_schedule_table_is_validated(lib):
     assert st == 0
     C = _lib.MemContractionConfig
     try:
-        good = (C * 3)(C(200, 0, 2, 0), C(640, 1, 4, 128), C(2 ** 31 - 1, 1, 2, 256))
+        good = (C * 3)(C(200, 0, 2, 0, 0, 0), C(640, 1, 4, 128, 256, 0),
+                       C(2 ** 31 - 1, 1, 2, 256, 128, 0))
         assert lib.mem_plan_set_contraction(h, 3, good) == _lib.MEM_OK
         for bad in ((C * 2)(C(640, 1, 2, 0), C(200, 1, 2, 0)),      # not increasing
                     (C * 2)(C(200, 2, 2, 0), C(640, 1, 2, 0)),      # persistent not 0/1
                     (C * 2)(C(200, 1, 3, 0), C(640, 1, 2, 0)),      # 3 accumulators
                     (C * 2)(C(200, 1, 2, 64), C(640, 1, 2, 0)),     # 64-wide tiles
-                    (C * 2)(C(200, 1, 4, 256), C(640, 1, 2, 0))):   # 4 x 256 TMEM columns
+                    (C * 2)(C(200, 1, 4, 256), C(640, 1, 2, 0)),    # 4 x 256 TMEM columns
+                    (C * 2)(C(200, 1, 2, 128, 192), C(640, 1, 2, 0)),   # 192-row tiles
+                    (C * 2)(C(200, 1, 2, 256, 256), C(640, 1, 2, 0))):  # 256 x 256
             assert lib.mem_plan_set_contraction(h, 2, bad) == _lib.MEM_ERR_INVALID
         assert lib.mem_plan_set_contraction(h, 0, good) == _lib.MEM_ERR_INVALID
         assert lib.mem_plan_set_wait_limit(h, 999) == _lib.MEM_ERR_INVALID

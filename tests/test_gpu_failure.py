@@ -50,15 +50,20 @@ def _status(plan):
     return plan.lib.mem_workspace_status(plan.handle, plan.workspace.data_ptr())
 
 
-def test_contraction_wait_runs_out_and_returns(cuda_ready, monkeypatch):
+@pytest.mark.parametrize('tile_m', ['128', '256'])
+def test_contraction_wait_runs_out_and_returns(cuda_ready, monkeypatch, tile_m):
+    """tile_m 256: the CTA-pair kernel (both CTAs' copies count on the even CTA's barriers)."""
     torch = cuda_ready
     from manifoldem_python_gb300 import _lib
     g = load_golden('config1')               # 300 images: three 128-row blocks, six tiles
     inp = _inputs(torch, g)
     good = _run(torch, _plan(torch, g, inp), inp)
     monkeypatch.setenv('MEM_TEST_WITHHOLD_CHUNK', '7')
+    monkeypatch.setenv('MEM_TC_TILE_M', tile_m)
+    monkeypatch.setenv('MEM_AUTOTUNE_CACHE', '/nonexistent/autotune.json')
     bad_plan = _plan(torch, g, inp)
     monkeypatch.delenv('MEM_TEST_WITHHOLD_CHUNK')
+    monkeypatch.delenv('MEM_TC_TILE_M')
     assert bad_plan.lib.mem_plan_set_wait_limit(bad_plan.handle, 200000) == _lib.MEM_OK
     assert bad_plan.lib.mem_plan_set_wait_limit(bad_plan.handle, 10) == _lib.MEM_ERR_INVALID
     _run(torch, bad_plan, inp)               # returns: every wait is bounded

@@ -1,6 +1,7 @@
 """Contraction schedules of the split-BF16 form (mem_plan_set_contraction): one CTA per tile or
 persistent CTAs walking several tiles, two or four TMEM accumulators, one or several size
-classes, 128- or 256-wide tiles.  Every schedule issues the same MMAs in the same order for
+classes, 128- or 256-wide tiles on one SM, 256 x 128 tiles on a pair of SMs
+(tcgen05.mma.cta_group::2).  Every schedule issues the same MMAs in the same order for
 every output element, so D must be bit-identical across schedules (and within 1e-6 of an FP64
 contraction, tested elsewhere)."""
 import numpy as np
@@ -52,6 +53,11 @@ def test_every_schedule_gives_the_same_D(cuda_ready):
         [dict(max_n=big, persistent=0, accumulators=2, tile_n=256)],
         [dict(max_n=200, persistent=1, accumulators=4, tile_n=128),
          dict(max_n=big, persistent=1, accumulators=2, tile_n=256)],
+        [dict(max_n=big, persistent=0, accumulators=2, tile_m=256)],
+        [dict(max_n=big, persistent=1, accumulators=4, tile_m=256)],
+        [dict(max_n=150, persistent=0, accumulators=2, tile_n=256),
+         dict(max_n=800, persistent=1, accumulators=2, tile_m=256),
+         dict(max_n=big, persistent=0, accumulators=4, tile_m=256)],
     ]
     ref = _run(torch, ds, sizes, schedules[0])
     assert np.isfinite(ref).all()

@@ -50,7 +50,11 @@ def _rank(rank, world, port, tmp, num_part, q):
     os.environ.update(MASTER_ADDR='127.0.0.1', MASTER_PORT=str(port), RANK=str(rank),
                       WORLD_SIZE=str(world))
     dist.init_process_group('gloo', rank=rank, world_size=world)
-    os.chdir(tmp)
+    # each rank's own working directory: the parameter file set_params writes there is
+    # per process, as on separate hosts
+    cwd = os.path.join(tmp, 'rank%d' % rank)
+    os.makedirs(cwd, exist_ok=True)
+    os.chdir(cwd)
     mp.init()
     mp.user_dir, mp.proj_name = tmp, 'rk'
     mp.create_dir()
@@ -89,8 +93,8 @@ def test_two_ranks_share_exactly_the_pending_pds(tmp_path):
         assert p.exitcode == 0
     shares = [r[1] for r in res]
     pending = sorted(set(range(N_PD)) - set(DONE_BEFORE))
-    assert not set(shares[0]) & set(shares[1])
-    assert sorted(shares[0] + shares[1]) == pending
+    assert not set(shares[0]) & set(shares[1]), shares
+    assert sorted(shares[0] + shares[1]) == pending, (shares, pending)
     assert all(shares)                                  # both ranks got work
     assert sorted(int(f) for f in os.listdir(prog)) == list(range(N_PD))
     for p, t in before.items():                         # finished PDs were not redone
