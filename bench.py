@@ -392,7 +392,9 @@ def kernels_per_execute(outputs, avg_only, N, counts=None, classes=None):
     (cuFFT transforms): lowpass_table, gather_normalize, lowpass_apply, rot_const, rotate,
     qfix, pd_sums, pd_finalize, features, [avg_store], [intensity], [contraction]."""
     smem = N in (32, 64, 128) and os.environ.get('MEM_SMEM_FFT', '1') != '0'
-    k = 9
+    # N = 64, 128: lowpass_fft, rotate and spectrum_fft are one image_stage kernel
+    fused = smem and N in (64, 128) and os.environ.get('MEM_FUSED_IMAGE', '0') == '1'
+    k = 7 if fused else 9
     if 'img_avg' in outputs or 'img_avg_flip' in outputs:
         k += 2 if smem else 1
     if smem and ('img_all_intensity' in outputs or 'img_all_flip' in outputs):
@@ -730,10 +732,16 @@ def roofline(r, args):
     per_img = {'gather': 2 * 4 * NN, 'lowpass': 2 * (4 * NN + 8 * Kc), 'rotate': 2 * 4 * NN,
                'spectrum': 4 * NN + 8 * Kc, 'sums': 8 * Kc, 'features': 8 * Kc + 16 * Kc + 8 * Kc,
                'averages': 0, 'flip': 8 * Kc + 4 * NN, }.get(dom, 4 * NN)
+    kernel = dom
+    if dom == 'lowpass' and ph.get('rotate', 0.0) < 1e-3 * ph['lowpass']:
+        # the fused image kernel (lowpass, rotate and spectrum phases in one launch): reads the
+        # raw image once and writes its half-plane spectrum once
+        per_img = 4 * NN + 8 * Kc
+        kernel = 'image_stage'
     b = per_img * r['n_images']
     ach = b / (ph[dom] * 1e-3) / 1e9
-    return dict(phase=dom, bound='hbm', achieved=ach, peak=peaks['hbm'], unit='GB/s',
-                frac=ach / peaks['hbm'], traffic=traffic_from_profiles(dom, args.config),
+    return dict(phase=kernel, bound='hbm', achieved=ach, peak=peaks['hbm'], unit='GB/s',
+                frac=ach / peaks['hbm'], traffic=traffic_from_profiles(kernel, args.config),
                 peak_source=peaks['src'] + ' hbm', algorithmic_bytes=b)
 
 
@@ -1094,7 +1102,13 @@ def main():
                     cuda_graph=r['graph']),
         roofline=dict(bound=rl['bound'], achieved=rl['achieved'], peak=rl['peak'],
                       unit=rl['unit'], frac=rl['frac'], traffic=rl['traffic'],
-                      kernel=rl['phase'], peak_source=rl['peak_source']),
+                      kernel=rl['phase'], peak_source=rl['peak_source'],
+                      traffic_source=(('profiles/%s_%s.md: ncu dram__bytes_read.sum + '
+                                       'dram__bytes_write.sum of the same kernel on a smaller '
+                                       'case, scaled to this launch by the work it covers')
+                                      % ((('contraction_' + args.precision) if
+                                          rl['phase'] == 'contraction' else rl['phase']),
+                                         args.config)) if rl['traffic'] else None),
         phases_ms=r['phases'],
         clocks=r['clocks'],
         gpu_launches=r['kernels'] * args.steps,

@@ -443,6 +443,8 @@ int mem_plan_create(const mem_params* params, int32_t n_pd, const int32_t* pd_co
     // cuFFT, for comparison)
     if (const char* e = std::getenv("MEM_SMEM_FFT")) P->smem_fft = std::atoi(e) != 0;
     P->smem_fft = P->smem_fft && kern::smem_fft_supported(*P);
+    if (const char* e = std::getenv("MEM_FUSED_IMAGE")) P->fused_image = std::atoi(e) != 0;
+    P->fused_image = P->fused_image && P->smem_fft && kern::image_stage_supported(*P);
     wait_settings_from_env(&P->wait_cycles, &P->test_withhold_chunk);
     if (const char* e = std::getenv("MEM_HOST_LOAD_CTAS")) P->host_load_ctas = std::atoi(e);
     if (const char* e = std::getenv("MEM_HOST_LOAD_THREADS")) {
@@ -692,10 +694,15 @@ int execute_impl(mem_plan* plan, const mem_inputs* in, const mem_outputs* out, v
         MEM_CUDA_TRY(cudaStreamWaitEvent(s, PM.load_done, 0));
         return MEM_OK;
     };
+    // the fused image kernel (N = 64, 128, no volume mask, SPIDER stack) writes each image's
+    // spectrum while other images are still being read: its input may not sit in the spectrum
+    // slots (a slot is larger than an image, so spectrum i overlaps later images' raw data)
+    const bool fused = P.fused_image && !in->pd_mask && !in->shift_yx;
     if (host_copy) {
-        // raw copies into free slots: xbuf when the RELION shift writes the spectrum slots,
-        // the spectrum slots otherwise
-        float* staging = in->shift_yx ? xbuf : reinterpret_cast<float*>(spec);
+        // raw copies into free slots: xbuf when the RELION shift writes the spectrum slots or
+        // the fused kernel writes them (image i's slot is read and rewritten by its own CTA
+        // only), the spectrum slots otherwise
+        float* staging = (in->shift_yx || fused) ? xbuf : reinterpret_cast<float*>(spec);
         MEM_STEP(kern::gather_copy(P, *in, staging, status, P.host_load_ctas, ls));
         MEM_STEP(join());
         cs = s;
@@ -712,7 +719,16 @@ int execute_impl(mem_plan* plan, const mem_inputs* in, const mem_outputs* out, v
         lin.num_stack = P.n_images;
         lin.stack_index = ident;
     }
-    if (P.smem_fft) {
+    float* img_all = out->img_all ? out->img_all : xbuf;
+    if (fused) {
+        // (a2-a4, a6, a8) gather, flip, normalisation, low-pass, mask, both rotations and
+        // F = fft2(imgAll) in one kernel per image; the lowpass phase holds all of it, the
+        // rotate and spectrum phases are empty
+        MEM_STEP(mark(1));
+        MEM_STEP(kern::rot_consts(P, *in, pds, img_pd, at<char>(ws, L.rotc), cs));
+        MEM_STEP(kern::image_stage(P, lin, at<float>(ws, L.gtab), at<float2>(ws, L.twid), xbuf,
+                                   img_all, at<char>(ws, L.rotc), spec, status, cs));
+    } else if (P.smem_fft) {
         // (a2, a3) gather, flip, normalisation and low-pass in one shared-memory pass
         MEM_STEP(mark(1));
         MEM_STEP(kern::lowpass_fused(P, lin, at<float>(ws, L.gtab), at<float2>(ws, L.twid), xbuf,
@@ -731,8 +747,8 @@ int execute_impl(mem_plan* plan, const mem_inputs* in, const mem_outputs* out, v
     }
     MEM_STEP(mark(2));
     // (a4, a6) mask and the two rotations -> imgAll
-    float* img_all = out->img_all ? out->img_all : xbuf;
-    MEM_STEP(kern::rotate(P, *in, xbuf, img_all, pds, img_pd, spec, at<char>(ws, L.rotc), s));
+    if (!fused)
+        MEM_STEP(kern::rotate(P, *in, xbuf, img_all, pds, img_pd, spec, at<char>(ws, L.rotc), s));
     MEM_STEP(mark(3));
     // (a8) F = fft2(imgAll); (a7, a9) CTF and per-PD sums.  With a volume mask the spectra of
     // D, of the phase flips and of imgAvgFlip are those of imgAll * msk2 (:344), while the Wiener
@@ -744,7 +760,7 @@ int execute_impl(mem_plan* plan, const mem_inputs* in, const mem_outputs* out, v
         return exec_fft(P, CUFFT_R2C, P.n_images, NN, specN, const_cast<float*>(images), spec,
                         work, s);
     };
-    MEM_STEP(spectrum(img_all));
+    if (!fused) MEM_STEP(spectrum(img_all));
     MEM_STEP(mark(4));
     MEM_STEP(kern::qfix(P, *in, qf, s));
     float* partial = at<float>(ws, L.partial);

@@ -28,8 +28,11 @@
 // owns 8 pair-rows and 8 columns, so only the row<->column hand-overs need a block barrier.
 // The position swizzle makes every shared-memory access of the four pass shapes conflict-free
 // for N = 128.
+#include <algorithm>
+
 #include "fft_radix.cuh"
 #include "mem_internal.cuh"
+#include "rotate_fixed.cuh"
 
 namespace mem {
 namespace {
@@ -130,17 +133,21 @@ struct Fft2 {
         }
     }
 
-    // image rows (2p, 2p+1) -> Z_p at natural positions (pass-1 shape; no statistics)
+    // image rows (2p, 2p+1) -> Z_p at natural positions (pass-1 shape; no statistics);
+    // COHERENT: src was written earlier in the same kernel (loads through L2, not the
+    // read-only path)
+    template <bool COHERENT = false>
     static __device__ __forceinline__ void load_rows(float2* S, const float* __restrict__ src) {
         const int w = warp(), l = lane();
+        auto ld = [&](const float* a) { return COHERENT ? __ldcg(a) : __ldg(a); };
 #pragma unroll 1
         for (int i = 0; i < IT1; ++i) {
             const int p = 8 * w + LP1 * i + l / R2, t = l % R2;
 #pragma unroll
             for (int m = 0; m < R1; ++m) {
                 const int b = t + R2 * m;
-                S[addr(p, b)] = make_float2(__ldg(src + (2 * p) * N + b),
-                                            __ldg(src + (2 * p + 1) * N + b));
+                S[addr(p, b)] = make_float2(ld(src + (2 * p) * N + b),
+                                            ld(src + (2 * p + 1) * N + b));
             }
         }
     }
@@ -524,6 +531,45 @@ __global__ void __launch_bounds__(2 * N, N == 128 ? 3 : 4) spectrum_fft_kernel(
     F::cols_spectrum_out(S, spec + img * (int64_t)N * F::HS);
 }
 
+// The image stage of one image in one CTA (N = 64, 128; no volume mask): gather + conjugate
+// flip + background normalisation + low-pass (lowpass_image), mask + the two periodic cubic
+// B-spline rotations (rot::rotate_image), and F = fft2(imgAll) written as the half-plane
+// spectrum -- the three kernels of the unfused path in one, so that the CTAs on an SM overlap
+// the FFTs' latency-bound passes with the rotation's shared-memory-bound sampling.  The
+// low-passed image and imgAll go through global memory (xbuf / img_out: L2-resident, read back
+// by the same CTA through L2); the shared buffer is reused by each phase.
+template <int N>
+__global__ void __launch_bounds__(2 * N, N == 128 ? 2 : 4) image_stage_kernel(
+        const float* __restrict__ stack, int64_t num_stack, const int64_t* __restrict__ sidx,
+        const uint8_t* __restrict__ flip, const float* __restrict__ gtab,
+        const float2* __restrict__ twid, float* xbuf, float* img_out,
+        const rot::RotConst* __restrict__ rotc, float2* __restrict__ spec,
+        uint32_t* __restrict__ status) {
+    using F = Fft2<N>;
+    constexpr int NT = 2 * N, NN = N * N;
+    extern __shared__ float2 S[];                      // FFT buffer, then rotation image
+    __shared__ float2 W[N];
+    __shared__ double red[2 * (NT / 32)];
+    __shared__ rot::RotConst rc[2];
+    __shared__ float carry[2 * rot::rot_nseg<NT, N>() * N];
+    const int64_t img = blockIdx.x;
+    F::twiddles(W, twid);
+    if (threadIdx.x < 2) rc[threadIdx.x] = rotc[2 * img + threadIdx.x];
+    float* xi = xbuf + img * (int64_t)NN;
+    float* out = img_out + img * (int64_t)NN;
+    lowpass_image<N>(img, S, W, red, stack, num_stack, sidx, flip, gtab, xbuf, status);
+    __syncthreads();                                   // xi written, S free
+    rot::rotate_image<NT, N, true>(xi, out, reinterpret_cast<float*>(S), carry, rc);
+    __syncthreads();                                   // imgAll written, S free
+    F::template load_rows<true>(S, out);
+    __syncthreads();
+    F::template rows_forward<false>(S, W, 0.f, 1.f);
+    __syncthreads();
+    F::cols_forward1(S, W);
+    __syncwarp();
+    F::cols_spectrum_out(S, spec + img * (int64_t)N * F::HS);
+}
+
 template <int N, bool SIGNED>
 __global__ void __launch_bounds__(2 * N, N == 128 ? 3 : 4) inverse_fft_kernel(
         const float2* __restrict__ spec, const float2* __restrict__ twid,
@@ -573,6 +619,32 @@ int lowpass_fused(const mem_plan& P, const mem_inputs& in, const float* gtab,
                 in.stack, in.num_stack, in.stack_index, in.flip, gtab, twid, xbuf, status);    \
     } while (0)
     MEM_FFT_DISPATCH(MEM_CALL)
+#undef MEM_CALL
+    MEM_LAUNCH_CHECK();
+    return MEM_OK;
+}
+
+bool image_stage_supported(const mem_plan& P) { return P.N == 64 || P.N == 128; }
+
+int image_stage(const mem_plan& P, const mem_inputs& in, const float* gtab, const float2* twid,
+                float* xbuf, float* img_out, const void* rotc, float2* spec, uint32_t* status,
+                cudaStream_t s) {
+    if (P.n_images == 0) return MEM_OK;
+    const rot::RotConst* rc = static_cast<const rot::RotConst*>(rotc);
+#define MEM_CALL(NV)                                                                           \
+    do {                                                                                       \
+        const size_t smem = std::max((size_t)(NV / 2) * NV * sizeof(float2),                   \
+                                     (size_t)(NV + 3) * rot::rot_stride<NV>() * sizeof(float)); \
+        if (prepare(image_stage_kernel<NV>, smem) != MEM_OK) return MEM_ERR_CUDA;              \
+        image_stage_kernel<NV><<<(unsigned)P.n_images, 2 * NV, smem, s>>>(                     \
+                in.stack, in.num_stack, in.stack_index, in.flip, gtab, twid, xbuf, img_out,    \
+                rc, spec, status);                                                             \
+    } while (0)
+    switch (P.N) {
+        case 64: MEM_CALL(64); break;
+        case 128: MEM_CALL(128); break;
+        default: return MEM_ERR_UNSUPPORTED;
+    }
 #undef MEM_CALL
     MEM_LAUNCH_CHECK();
     return MEM_OK;

@@ -127,6 +127,10 @@ struct mem_plan {
     bool tc_kahan = false;          // compensated register sums across groups
     bool tc_lolo = false;           // add the lo.lo product (4-term split)
     bool smem_fft = true;           // shared-memory FFT kernels instead of cuFFT (N = 32, 64, 128)
+    // N = 64, 128 without a volume mask: low-pass, rotations and spectrum in one kernel
+    // (MEM_FUSED_IMAGE=1; off by default: measured slower than the three kernels, see
+    // image_stage_kernel)
+    bool fused_image = false;
     // host-to-device image copy of a split execute: the fewer SMs it occupies the less it slows
     // the concurrent computation; 8 x 1024 threads, two images per step, keep ~1 MB of loads in
     // flight, enough for the host link
@@ -185,6 +189,15 @@ int spectrum_fft(const mem_plan& P, int64_t count, const float* images, const fl
 // signed = the phase-flip inverse: element k of image i multiplied by sign(C_i(k)) / N^2 on load
 int inverse_fft(const mem_plan& P, int64_t count, const float2* spec, const float2* twid,
                 float* images, const uint64_t* qf, bool signed_flip, cudaStream_t s);
+// the two rotations' fixed-point constants of every image into rot_scratch (64 bytes each)
+int rot_consts(const mem_plan& P, const mem_inputs& in, const PdDev* pd_table,
+               const int32_t* img_pd, void* rot_scratch, cudaStream_t s);
+// N = 64, 128: gather + flip + normalisation + low-pass, mask + both rotations and the spectrum
+// of imgAll in one kernel (rot_consts first); img_out receives imgAll, spec the spectra
+bool image_stage_supported(const mem_plan& P);
+int image_stage(const mem_plan& P, const mem_inputs& in, const float* gtab, const float2* twid,
+                float* xbuf, float* img_out, const void* rotc, float2* spec, uint32_t* status,
+                cudaStream_t s);
 // rot_scratch: 64 bytes per image (the two rotations' fixed-point constants)
 int rotate(const mem_plan& P, const mem_inputs& in, float* xbuf, float* img_out,
            const PdDev* pd_table, const int32_t* img_pd, float2* spec, void* rot_scratch,

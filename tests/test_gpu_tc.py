@@ -162,3 +162,36 @@ def test_ring_features_match_per_frequency(cuda_ready, N, precision):
     # both forms sit near 1e-6 of the FP64 contraction at 128 px)
     assert e < 2e-6 and e64 < max(1.25 * e64_pf, 1e-6)
     np.testing.assert_array_equal(res[1]['D'], res[1]['D'].T)
+
+
+@pytest.mark.parametrize('N', [64, 128])
+def test_fused_image_stage_matches_three_kernels(cuda_ready, N):
+    """The fused per-image kernel (low-pass, both rotations and the spectrum in one CTA per
+    image) against the three separate kernels on the same inputs: every output of the stage.
+    The fused kernel runs the rotation with twice the samples per thread (prefilter segments of
+    2x the length, start states truncated at a smaller power of the pole), so the outputs agree
+    to rounding, not bit for bit."""
+    torch = cuda_ready
+    from manifoldem_python_gb300.pipeline import DistanceStage, PdJob, StageParams
+    cfg, ds = _dataset(N, 60, conj=0.5, seed=52 + N)
+    names = ('D', 'img_all', 'img_all_flip', 'img_avg', 'img_avg_flip', 'img_all_intensity',
+             'spectrum', 'ctf')
+    outs = {}
+    for fused in (0, 1):
+        old = os.environ.get('MEM_FUSED_IMAGE')
+        os.environ['MEM_FUSED_IMAGE'] = str(fused)
+        try:
+            st = DistanceStage(StageParams(N=cfg.N, pix_size=cfg.pix, Cs=cfg.cs, EkV=cfg.kv,
+                                           AmpContrast=cfg.ampc, precision='bf16x3'))
+            ind = ds.CG[0]
+            outs[fused] = st.run([PdJob(ind=ind, q=ds.q[:, ind], df=ds.df[ind])],
+                                 ds.stack.to('cuda'), ds.nStot, outputs=names)[0]
+        finally:
+            if old is None:
+                os.environ.pop('MEM_FUSED_IMAGE', None)
+            else:
+                os.environ['MEM_FUSED_IMAGE'] = old
+    for k in names:
+        e = rel(np.asarray(outs[1][k]), np.asarray(outs[0][k]))
+        print('N=%d %s: fused vs three kernels %.3g' % (N, k, e))
+        assert e < 1e-6, (k, e)
