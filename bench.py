@@ -585,16 +585,20 @@ def run_gpu(args, rank, world):
             torch.cuda.empty_cache()
             st = StreamedStage(params, counts, [g.psi_p for g in geoms], n_groups=args.e2e_groups,
                                outputs=res_names, device=dev, ramp=args.e2e_ramp,
-                               ramp_steps=args.e2e_ramp_steps)
+                               ramp_steps=args.e2e_ramp_steps, dma=args.e2e_dma)
             st.set_metadata(sidx_h, flip_h, psi_h, df_h)
-            h2d = stack_h.numel() * 4 + st.metadata_bytes()
+            h2d = st.image_bytes(stack_h.shape[0]) + st.metadata_bytes()
             d2h = st.result_bytes()
 
             def e2e_step():
                 st.run(stack_h)
-            mode = 'streamed: stack in pinned host memory read by the load kernels over the host ' \
-                   'link, %d PD groups (image counts %s) on load / compute / copy streams' % (
-                       len(st.groups), [int(sum(counts[i] for i in g)) for g in st.groups])
+            staged = st.staged_groups()
+            how = ('%d of them staged by the copy engines (contiguous stack ranges), the rest '
+                   'read by the load kernel over the host link' % staged) if staged else \
+                'read by the load kernel over the host link'
+            mode = 'streamed: stack in pinned host memory, %d PD groups (image counts %s), %s, ' \
+                   'on load / compute / copy streams' % (
+                       len(st.groups), [int(sum(counts[i] for i in g)) for g in st.groups], how)
         else:
             meta_h = [torch.from_numpy(x).pin_memory() if pin else torch.from_numpy(x)
                       for x in (sidx_h, flip_h, psi_h, df_h)]
@@ -1000,6 +1004,10 @@ def main():
     ap.add_argument('--e2e-ramp', type=float, default=1.35,
                     help='growth factor of the first PD groups of the streamed e2e pass')
     ap.add_argument('--e2e-ramp-steps', type=int, default=5)
+    ap.add_argument('--e2e-dma', default='auto', choices=['auto', 'off'],
+                    help='streamed e2e: auto = groups whose images are a few contiguous stack '
+                         'ranges are copied by the copy engines into staging buffers; off = '
+                         'every group read over the host link by the load kernel')
     ap.add_argument('--no-dm', action='store_true',
                     help='skip the diffusion-map embedding of a sample of PDs (GPU vs CPU port)')
     ap.add_argument('--dm-pds', type=int, default=8)

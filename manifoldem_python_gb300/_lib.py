@@ -22,7 +22,7 @@ INCLUDE = os.path.join(REPO, 'include')
 BUILD_DIR = os.path.join(REPO, '_build')
 LIB_PATH = os.path.join(HERE, 'libmanifoldem_gb300.so')
 SOURCES = ['abi.cu', 'prologue.cu', 'gemm_fp32.cu', 'gemm_tc.cu', 'noalloc.cu', 'image_fft.cu',
-           'dmap.cu', 'relion.cu', 'mask.cu', 'nlsa.cu']
+           'dmap.cu', 'relion.cu', 'mask.cu', 'nlsa.cu', 'rotate_band.cu']
 ARCH_FLAGS = ['-gencode', 'arch=compute_103a,code=sm_103a']
 
 # status codes (include/manifoldem_gb300.h)

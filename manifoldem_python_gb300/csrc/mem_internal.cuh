@@ -131,6 +131,9 @@ struct mem_plan {
     // (MEM_FUSED_IMAGE=1; off by default: measured slower than the three kernels, see
     // image_stage_kernel)
     bool fused_image = false;
+    // boxes rotated by rotate_band: 1 = N > 236 (no whole-image shared-memory kernel), 2 = also
+    // N <= 236 without a compile-time kernel, 0 = never (MEM_ROT_BAND)
+    int rot_band = 1;
     // host-to-device image copy of a split execute: the fewer SMs it occupies the less it slows
     // the concurrent computation; 8 x 1024 threads, two images per step, keep ~1 MB of loads in
     // flight, enough for the host link
@@ -202,6 +205,11 @@ int image_stage(const mem_plan& P, const mem_inputs& in, const float* gtab, cons
 int rotate(const mem_plan& P, const mem_inputs& in, float* xbuf, float* img_out,
            const PdDev* pd_table, const int32_t* img_pd, float2* spec, void* rot_scratch,
            cudaStream_t s);
+// the two rotations with the coefficient image in bands of rows (64 <= N <= 512; rotate calls it
+// for boxes without a shared-memory kernel); spec is the coefficient scratch
+bool rotate_band_supported(int N);
+int rotate_band(const mem_plan& P, float* xbuf, float2* spec, float* img_out, const void* rotc,
+                cudaStream_t s);
 int qfix(const mem_plan& P, const mem_inputs& in, uint64_t* qf, cudaStream_t s);
 // which: 1 = S0..S2, 2 = S3..S5, 3 = all six per-PD sums
 int pd_sums(const mem_plan& P, const float2* spec, const uint64_t* qf, const SumItem* items,

@@ -401,15 +401,6 @@ __device__ void prefilter_axis(float* s, int N, int P, int axis, int nseg, float
     __syncthreads();
 }
 
-__device__ __forceinline__ void bspline_w(float t, float w[4]) {
-    const float u = 1.0f - t;
-    const float t2 = t * t, u2 = u * u;
-    w[0] = (1.0f / 6.0f) * u2 * u;
-    w[3] = (1.0f / 6.0f) * t2 * t;
-    w[1] = (2.0f / 3.0f) - t2 * (1.0f - 0.5f * t);
-    w[2] = (2.0f / 3.0f) - u2 * (1.0f - 0.5f * u);
-}
-
 // wrapped index of i in [-N, 2N)
 __device__ __forceinline__ int wrapN(int i, int N) {
     i += (i < 0) ? N : 0;
@@ -1048,6 +1039,10 @@ int rotate(const mem_plan& P, const mem_inputs& in, float* xbuf, float* img_out,
     RotConst* rotc = static_cast<RotConst*>(rot_scratch);
     const int st = rot_consts(P, in, pd_table, img_pd, rot_scratch, s);
     if (st != MEM_OK) return st;
+    const bool fixed_n = N == 64 || N == 128;
+    if (kern::rotate_band_supported(N) &&
+        ((P.rot_band >= 1 && N > kMaxSmemN) || (P.rot_band >= 2 && !fixed_n)))
+        return kern::rotate_band(P, xbuf, spec, img_out, rotc, s);
     if (N > kMaxSmemN) {
         constexpr int NT = 512;
         const int nseg = std::max(1, std::min(NT / N, N / 16));

@@ -138,6 +138,16 @@ __device__ __forceinline__ void prefilter_fixed(float* s, float* carry,
     __syncthreads();
 }
 
+// Cubic B-spline weights of the 4-tap window at fractional offset t in [0, 1)
+__device__ __forceinline__ void bspline_w(float t, float w[4]) {
+    const float u = 1.0f - t;
+    const float t2 = t * t, u2 = u * u;
+    w[0] = (1.0f / 6.0f) * u2 * u;
+    w[3] = (1.0f / 6.0f) * t2 * t;
+    w[1] = (2.0f / 3.0f) - t2 * (1.0f - 0.5f * t);
+    w[2] = (2.0f / 3.0f) - u2 * (1.0f - 0.5f * u);
+}
+
 // Two output samples a, b at once with paired FP32 instructions (fma.rn.f32x2 and friends);
 // per sample the same operations in the same order as bspline_w / sample_fixed.
 __device__ __forceinline__ void bspline_w2(float2 t, float2 w[4]) {

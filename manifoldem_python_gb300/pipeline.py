@@ -353,6 +353,23 @@ def group_weights(n_groups: int, ramp: float = 1.0, ramp_steps: int = 0) -> np.n
     return float(ramp) ** np.minimum(g, max(0, int(ramp_steps)))
 
 
+def stack_runs(stack_index, max_runs: int):
+    """The distinct stack indices of a group as runs of consecutive indices: (runs, remap) with
+    runs = [(first index, count, offset in the staged copy)] and remap = each entry's position
+    in the staged copy, or None when there are more than ``max_runs`` runs."""
+    si = np.asarray(stack_index, dtype=np.int64)
+    if si.size == 0:
+        return [], si.copy()
+    u = np.unique(si)
+    breaks = np.nonzero(np.diff(u) != 1)[0] + 1
+    if breaks.size + 1 > max_runs:
+        return None
+    starts = np.concatenate([[0], breaks])
+    ends = np.concatenate([breaks, [u.size]])
+    runs = [(int(u[a]), int(b - a), int(a)) for a, b in zip(starts, ends)]
+    return runs, np.searchsorted(u, si).astype(np.int64)
+
+
 def balanced_groups(counts: Sequence[int], n_groups: int, ramp: float = 1.0,
                     ramp_steps: int = 0) -> List[range]:
     """Consecutive PD ranges (at most n_groups, none empty) whose image counts follow
@@ -379,16 +396,26 @@ class StreamedStage:
     128 px the host link delivers images about 1.3x faster than the stage computes them (0.31 us
     against 0.41 us per image on a GB300), so each group may be up to about that much larger than
     the one before without the compute stream waiting, and a small first group shortens the wait
-    before the first computation.  Every ``run`` issues, per group, the per-image metadata copy and the stack-reading
-    kernel on a high-priority load stream (a small grid reading the images over the host link,
-    ``mem_plan_execute_split``), the rest of the stage on a compute stream, and the copy of the
-    results into pinned host buffers on a copy stream.  Group g+1's images arrive while group g
-    computes, and group g's results leave while group g+1 computes.
+    before the first computation.  Every ``run`` issues, per group, the per-image metadata copy and
+    the image copy on a high-priority load stream, the rest of the stage on a compute stream, and
+    the copy of the results into pinned host buffers on a copy stream.  Group g+1's images arrive
+    while group g computes, and group g's results leave while group g+1 computes.
+
+    The image copy: a group whose images form at most ``max_runs`` runs of consecutive stack
+    indices (a stack stored in PD order) is copied run by run by the copy engines into a device
+    staging buffer of its own, and its plan executes on the staged images (``dma='auto'``); any
+    other group is read by a small grid of the library's load kernel over the host link
+    (``mem_plan_execute_split``), which gathers scattered images without staging the stack
+    (``dma='off'`` for every group).
     """
 
     def __init__(self, params: StageParams, counts: Sequence[int], psi_p: Sequence[float],
                  n_groups: int = 11, outputs=('D', 'img_avg', 'img_avg_flip', 'img_all_intensity'),
-                 device=None, ramp: float = 1.35, ramp_steps: int = 5):
+                 device=None, ramp: float = 1.35, ramp_steps: int = 5, dma: str = 'auto',
+                 max_runs: int = 64):
+        if dma not in ('auto', 'off'):
+            raise ValueError("dma must be 'auto' or 'off'")
+        self.dma, self.max_runs = dma, int(max_runs)
         import torch
         self.device = torch.device(device or 'cuda')
         self.counts = [int(c) for c in counts]
@@ -416,14 +443,49 @@ class StreamedStage:
                   np.ascontiguousarray(flip, dtype=np.uint8),
                   np.ascontiguousarray(psi_rad, dtype=np.float64),
                   np.ascontiguousarray(df, dtype=np.float64)]
-        self._meta_h, self._meta_d = [], []
+        self._meta_h, self._meta_d, self._runs, self._staging = [], [], [], []
+        self._remap_h, self._remap_d = [], []
+        N = self.plans[0].params.N if self.plans else 0
         for a, b in self.img_ranges:
-            hs = [torch.from_numpy(x[a:b].copy()).pin_memory() for x in arrays]
+            sel = [x[a:b].copy() for x in arrays]
+            found = stack_runs(sel[0], self.max_runs) if self.dma == 'auto' else None
+            runs, remap_h, remap_d, staging = None, None, None, None
+            if found is not None:
+                runs, remap = found
+                remap_h = torch.from_numpy(remap).pin_memory()
+                remap_d = torch.empty_like(remap_h, device=self.device)
+                staging = torch.empty((sum(r[1] for r in runs), N, N), dtype=torch.float32,
+                                      device=self.device)
+            self._runs.append(runs)
+            self._remap_h.append(remap_h)
+            self._remap_d.append(remap_d)
+            self._staging.append(staging)
+            hs = [torch.from_numpy(x).pin_memory() for x in sel]
             self._meta_h.append(hs)
             self._meta_d.append([torch.empty_like(h, device=self.device) for h in hs])
 
     def metadata_bytes(self) -> int:
-        return sum(t.numel() * t.element_size() for hs in self._meta_h for t in hs)
+        """Per-image metadata bytes one run copies (staged groups: their staging indices in
+        place of the stack indices)."""
+        total = 0
+        for hs, rh in zip(self._meta_h, self._remap_h):
+            ts = hs if rh is None else [rh] + list(hs[1:])
+            total += sum(t.numel() * t.element_size() for t in ts)
+        return total
+
+    def staged_groups(self) -> int:
+        """Groups whose images the copy engines stage (the rest use the load kernel)."""
+        return sum(r is not None for r in self._runs)
+
+    def image_bytes(self, num_stack: int) -> int:
+        """Image bytes one run copies to the device: the staged runs, and for the other groups
+        the entries' images (read once each by the load kernel)."""
+        N = self.plans[0].params.N if self.plans else 0
+        total = 0
+        for g, (a, b) in enumerate(self.img_ranges):
+            n = sum(r[1] for r in self._runs[g]) if self._runs[g] is not None else b - a
+            total += n * N * N * 4
+        return total
 
     def result_bytes(self) -> int:
         return sum(t.numel() * t.element_size() for d in self.host_out for t in d.values())
@@ -437,13 +499,28 @@ class StreamedStage:
         cur = torch.cuda.current_stream(self.device)
         for s in (self.load_stream, self.stream, self.copy_stream):
             s.wait_stream(cur)
+        host_stack = not stack.is_cuda
         for g, plan in enumerate(self.plans):
+            staged = host_stack and self._runs[g] is not None
             with torch.cuda.stream(self.load_stream):
-                for dst, src in zip(self._meta_d[g], self._meta_h[g]):
-                    dst.copy_(src, non_blocking=True)
+                for i, (dst, src) in enumerate(zip(self._meta_d[g], self._meta_h[g])):
+                    if not (staged and i == 0):          # staged: the staging indices instead
+                        dst.copy_(src, non_blocking=True)
+                if staged:
+                    self._remap_d[g].copy_(self._remap_h[g], non_blocking=True)
+                    buf = self._staging[g]
+                    for first, count, off in self._runs[g]:
+                        buf[off:off + count].copy_(stack[first:first + count], non_blocking=True)
             sidx, flip, psi, df = self._meta_d[g]
-            plan.execute_split(stack, sidx, flip, psi, df, self.dev_out[g], self.load_stream,
-                               self.stream)
+            if staged:
+                loaded = torch.cuda.Event()
+                loaded.record(self.load_stream)
+                self.stream.wait_event(loaded)
+                plan.execute(self._staging[g], self._remap_d[g], flip, psi, df, self.dev_out[g],
+                             self.stream)
+            else:
+                plan.execute_split(stack, sidx, flip, psi, df, self.dev_out[g],
+                                   self.load_stream, self.stream)
             done = torch.cuda.Event()
             done.record(self.stream)
             self.copy_stream.wait_event(done)

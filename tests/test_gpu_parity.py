@@ -174,9 +174,13 @@ def test_box_sizes_match_oracle(cuda_ready, N):
         assert rel(res['D'], ref['D']) < 1e-5
 
 
-def test_streamed_stage_matches_plain(cuda_ready):
-    """StreamedStage (stack in pinned host memory, PD groups on load / compute / copy streams,
-    mem_plan_execute_split) against one plain execute with the stack on the device."""
+@pytest.mark.parametrize('dma,shuffle', [('off', False), ('auto', False), ('auto', True)])
+def test_streamed_stage_matches_plain(cuda_ready, dma, shuffle):
+    """StreamedStage (stack in pinned host memory, PD groups on load / compute / copy streams)
+    against one plain execute with the stack on the device: every group read by the load
+    kernel (dma off, mem_plan_execute_split), every group staged by the copy engines (the
+    synthetic stack is in PD order), and a stack in shuffled order whose groups have more runs
+    than the limit (load kernel) or fewer (staged)."""
     torch = cuda_ready
     import dataclasses
     from manifoldem_python_gb300.geometry import pd_geometry
@@ -194,12 +198,26 @@ def test_streamed_stage_matches_plain(cuda_ready):
         ref = DistanceStage(params).run(jobs, ds.stack.cuda(), ds.nStot, outputs=names)
         geoms = [pd_geometry(np.asarray(j.ind), j.q, ds.nStot) for j in jobs]
         counts = [len(j.ind) for j in jobs]
-        st = StreamedStage(params, counts, [g.psi_p for g in geoms], n_groups=3, outputs=names)
-        st.set_metadata(np.concatenate([g.stack_index for g in geoms]),
+        st = StreamedStage(params, counts, [g.psi_p for g in geoms], n_groups=3, outputs=names,
+                           dma=dma, max_runs=64 if not shuffle else 40)
+        sidx = np.concatenate([g.stack_index for g in geoms])
+        stack_h = ds.stack.contiguous().pin_memory()
+        if shuffle:
+            # the same images in a permuted stack, each entry pointed at its image's new place
+            num = ds.stack.shape[0]
+            perm = np.random.default_rng(N).permutation(num)
+            inv = np.empty_like(perm)
+            inv[perm] = np.arange(num)
+            stack_h = ds.stack[torch.from_numpy(perm)].contiguous().pin_memory()
+            sidx = inv[sidx]
+        st.set_metadata(sidx,
                         np.concatenate([g.flip for g in geoms]),
                         np.concatenate([g.psi_rad for g in geoms]),
                         np.concatenate([np.asarray(j.df, np.float64) for j in jobs]))
-        stack_h = ds.stack.contiguous().pin_memory()
+        if dma == 'off':
+            assert st.staged_groups() == 0
+        elif not shuffle:
+            assert st.staged_groups() == len(st.groups)
         for _ in range(2):                      # two runs in a row reuse every buffer
             host = st.run(stack_h)
         st.device_status()

@@ -195,3 +195,35 @@ def test_fused_image_stage_matches_three_kernels(cuda_ready, N):
         e = rel(np.asarray(outs[1][k]), np.asarray(outs[0][k]))
         print('N=%d %s: fused vs three kernels %.3g' % (N, k, e))
         assert e < 1e-6, (k, e)
+
+
+@pytest.mark.parametrize('N', [96, 250, 300, 512])
+def test_band_rotation_matches_whole_image_kernels(cuda_ready, N):
+    """The banded rotation (coefficient image in bands of rows in shared memory, the column
+    prefilter through global memory) against the whole-image kernels on the same inputs
+    (MEM_ROT_BAND=0: the shared-memory kernel for N <= 236, the global-memory one above): imgAll
+    and D agree to rounding (the two prefilters truncate their periodic start sums differently
+    and filter the second rotation's axes in the other order)."""
+    torch = cuda_ready
+    from manifoldem_python_gb300.pipeline import DistanceStage, PdJob, StageParams
+    cfg, ds = _dataset(N, 12, conj=0.5, seed=70 + N)
+    names = ('D', 'img_all', 'img_all_flip', 'img_avg')
+    outs = {}
+    for band in (0, 2):
+        old = os.environ.get('MEM_ROT_BAND')
+        os.environ['MEM_ROT_BAND'] = str(band)
+        try:
+            st = DistanceStage(StageParams(N=cfg.N, pix_size=cfg.pix, Cs=cfg.cs, EkV=cfg.kv,
+                                           AmpContrast=cfg.ampc, precision='bf16x3'))
+            ind = ds.CG[0]
+            outs[band] = st.run([PdJob(ind=ind, q=ds.q[:, ind], df=ds.df[ind])],
+                                ds.stack.to('cuda'), ds.nStot, outputs=names)[0]
+        finally:
+            if old is None:
+                os.environ.pop('MEM_ROT_BAND', None)
+            else:
+                os.environ['MEM_ROT_BAND'] = old
+    for k in names:
+        e = rel(np.asarray(outs[2][k]), np.asarray(outs[0][k]))
+        print('N=%d %s: banded vs whole-image rotation %.3g' % (N, k, e))
+        assert e < 2e-6, (k, e)

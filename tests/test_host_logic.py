@@ -141,3 +141,20 @@ def test_mrc_round_trip(tmp_path):
     path2 = str(tmp_path / 'b.mrcs')
     open(path2, 'wb').write(bytes(raw))
     np.testing.assert_array_equal(np.asarray(mrc.read_stack(path2)), data)
+
+
+def test_stack_runs_split_and_remap():
+    """Runs of consecutive stack indices for the copy-engine staging of a streamed group, and
+    each entry's position in the staged copy (duplicates, any order)."""
+    from manifoldem_python_gb300.pipeline import stack_runs
+    si = np.array([5, 6, 7, 7, 20, 21, 9, 6])
+    runs, remap = stack_runs(si, 8)
+    assert runs == [(5, 3, 0), (9, 1, 3), (20, 2, 4)]
+    staged = np.concatenate([np.arange(f, f + c) for f, c, _ in runs])
+    np.testing.assert_array_equal(staged[remap], si)
+    assert stack_runs(si, 2) is None
+    runs, remap = stack_runs(np.arange(100)[::-1], 1)
+    assert runs == [(0, 100, 0)]
+    np.testing.assert_array_equal(remap, np.arange(100)[::-1])
+    runs, remap = stack_runs(np.array([], dtype=np.int64), 1)
+    assert runs == [] and remap.size == 0
