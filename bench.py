@@ -1004,10 +1004,11 @@ def main():
     ap.add_argument('--e2e-ramp', type=float, default=1.35,
                     help='growth factor of the first PD groups of the streamed e2e pass')
     ap.add_argument('--e2e-ramp-steps', type=int, default=5)
-    ap.add_argument('--e2e-dma', default='auto', choices=['auto', 'off'],
-                    help='streamed e2e: auto = groups whose images are a few contiguous stack '
-                         'ranges are copied by the copy engines into staging buffers; off = '
-                         'every group read over the host link by the load kernel')
+    ap.add_argument('--e2e-dma', default='off', choices=['auto', 'off'],
+                    help='streamed e2e: off = every group read over the host link by the load '
+                         'kernel; auto = groups whose images are a few contiguous stack ranges '
+                         'are copied by the copy engines into staging buffers (slower on GB300: '
+                         '207 against 170 ms per config4 pass)')
     ap.add_argument('--no-dm', action='store_true',
                     help='skip the diffusion-map embedding of a sample of PDs (GPU vs CPU port)')
     ap.add_argument('--dm-pds', type=int, default=8)

@@ -446,6 +446,8 @@ int mem_plan_create(const mem_params* params, int32_t n_pd, const int32_t* pd_co
     if (const char* e = std::getenv("MEM_FUSED_IMAGE")) P->fused_image = std::atoi(e) != 0;
     P->fused_image = P->fused_image && P->smem_fft && kern::image_stage_supported(*P);
     if (const char* e = std::getenv("MEM_ROT_BAND")) P->rot_band = std::atoi(e);
+    if (const char* e = std::getenv("MEM_ROT_BAND_VARIANT"))
+        P->rot_band_variant = std::min(3, std::max(0, std::atoi(e)));
     wait_settings_from_env(&P->wait_cycles, &P->test_withhold_chunk);
     if (const char* e = std::getenv("MEM_HOST_LOAD_CTAS")) P->host_load_ctas = std::atoi(e);
     if (const char* e = std::getenv("MEM_HOST_LOAD_THREADS")) {

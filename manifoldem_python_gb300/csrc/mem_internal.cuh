@@ -134,6 +134,7 @@ struct mem_plan {
     // boxes rotated by rotate_band: 1 = N > 236 (no whole-image shared-memory kernel), 2 = also
     // N <= 236 without a compile-time kernel, 0 = never (MEM_ROT_BAND)
     int rot_band = 1;
+    int rot_band_variant = 2;       // rotate_band's sampling / occupancy form (MEM_ROT_BAND_VARIANT)
     // host-to-device image copy of a split execute: the fewer SMs it occupies the less it slows
     // the concurrent computation; 8 x 1024 threads, two images per step, keep ~1 MB of loads in
     // flight, enough for the host link

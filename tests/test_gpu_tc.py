@@ -209,21 +209,24 @@ def test_band_rotation_matches_whole_image_kernels(cuda_ready, N):
     cfg, ds = _dataset(N, 12, conj=0.5, seed=70 + N)
     names = ('D', 'img_all', 'img_all_flip', 'img_avg')
     outs = {}
-    for band in (0, 2):
-        old = os.environ.get('MEM_ROT_BAND')
+    for band, variant in ((0, 0), (2, 0), (2, 1), (2, 2), (2, 3)):
+        old = {k: os.environ.get(k) for k in ('MEM_ROT_BAND', 'MEM_ROT_BAND_VARIANT')}
         os.environ['MEM_ROT_BAND'] = str(band)
+        os.environ['MEM_ROT_BAND_VARIANT'] = str(variant)
         try:
             st = DistanceStage(StageParams(N=cfg.N, pix_size=cfg.pix, Cs=cfg.cs, EkV=cfg.kv,
                                            AmpContrast=cfg.ampc, precision='bf16x3'))
             ind = ds.CG[0]
-            outs[band] = st.run([PdJob(ind=ind, q=ds.q[:, ind], df=ds.df[ind])],
-                                ds.stack.to('cuda'), ds.nStot, outputs=names)[0]
+            outs[band, variant] = st.run([PdJob(ind=ind, q=ds.q[:, ind], df=ds.df[ind])],
+                                         ds.stack.to('cuda'), ds.nStot, outputs=names)[0]
         finally:
-            if old is None:
-                os.environ.pop('MEM_ROT_BAND', None)
-            else:
-                os.environ['MEM_ROT_BAND'] = old
-    for k in names:
-        e = rel(np.asarray(outs[2][k]), np.asarray(outs[0][k]))
-        print('N=%d %s: banded vs whole-image rotation %.3g' % (N, k, e))
-        assert e < 2e-6, (k, e)
+            for k, v in old.items():
+                if v is None:
+                    os.environ.pop(k, None)
+                else:
+                    os.environ[k] = v
+    for variant in (0, 1, 2, 3):
+        for k in names:
+            e = rel(np.asarray(outs[2, variant][k]), np.asarray(outs[0, 0][k]))
+            print('N=%d variant %d %s: banded vs whole-image rotation %.3g' % (N, variant, k, e))
+            assert e < 2e-6, (variant, k, e)
