@@ -427,33 +427,38 @@ __device__ __forceinline__ float sample_at(const float* s, int N, int P, int64_t
 }
 
 // Thread t owns column c = t % N and rows r = t / N + k R (R = NT / N rows per pass), so its
-// sample coordinates advance by a constant fixed-point step.
+// sample coordinates advance by a constant fixed-point step.  A warp's lanes sample along an
+// output row, a step of (rs, rc) in (x, y); tap (ix, iy) sits in bank (ix P + iy) mod 32, so each
+// rotation lays its coefficient image out with row stride P1 = 1 mod 32 when rc and rs have one
+// sign and Pm1 = -1 mod 32 otherwise (a monotone bank index across the lanes: about two
+// wavefronts per tap instruction); P1 = Pm1 = an odd stride where those do not fit.
 template <int NT, int MAXV>
 __global__ void __launch_bounds__(NT) rotate_kernel(
         float* __restrict__ xbuf, float* __restrict__ img_out, const RotConst* __restrict__ rotc,
-        int N, int P, int nseg, float inv1mzN, int exact_init) {
+        int N, int P1, int Pm1, int nseg, float inv1mzN, int exact_init) {
     extern __shared__ float s[];
-    __shared__ RotConst rot[2];
     const int64_t img = blockIdx.x;
+    const RotConst q0 = rotc[2 * img], q1 = rotc[2 * img + 1];
+    const int Pa = (q0.rc > 0) == (q0.rs > 0) ? P1 : Pm1;
+    const int Pb = (q1.rc > 0) == (q1.rs > 0) ? P1 : Pm1;
     const int NN = N * N;
     float* xi = xbuf + img * (int64_t)NN;
     const int R = NT / N;                       // rows per pass
     const int c = threadIdx.x % N;
     const int r0 = threadIdx.x / N;
     const bool active = r0 < R;
-    if (threadIdx.x < 2) rot[threadIdx.x] = rotc[2 * img + threadIdx.x];
     // load (storage orientation) into smem in reference orientation, times the mask
     for (int p = threadIdx.x; p < NN; p += NT) {
         const int a = p / N, b = p - a * N;
-        s[b * P + a] = xi[p] * mask_ref(b, a, N);
+        s[b * Pa + a] = xi[p] * mask_ref(b, a, N);
     }
     __syncthreads();
-    prefilter_axis<NT>(s, N, P, 0, nseg, inv1mzN, exact_init != 0);
-    prefilter_axis<NT>(s, N, P, 1, nseg, inv1mzN, exact_init != 0);
-    fill_halo<NT>(s, N, P);
+    prefilter_axis<NT>(s, N, Pa, 0, nseg, inv1mzN, exact_init != 0);
+    prefilter_axis<NT>(s, N, Pa, 1, nseg, inv1mzN, exact_init != 0);
+    fill_halo<NT>(s, N, Pa);
     float keep[MAXV > 0 ? MAXV : 1];
     {
-        const RotConst Q = rot[0];
+        const RotConst& Q = q0;
         int64_t X = Q.bx + (int64_t)r0 * Q.rc + (int64_t)c * Q.rs;
         int64_t Y = Q.by - (int64_t)r0 * Q.rs + (int64_t)c * Q.rc;
         const int64_t dX = (int64_t)R * Q.rc, dY = -(int64_t)R * Q.rs;
@@ -461,12 +466,13 @@ __global__ void __launch_bounds__(NT) rotate_kernel(
 #pragma unroll
             for (int k = 0; k < MAXV; ++k) {
                 const int r = r0 + k * R;
-                if (active && r < N) keep[k] = sample_at(s, N, P, X, Y);
+                if (active && r < N) keep[k] = sample_at(s, N, Pa, X, Y);
                 X += dX;
                 Y += dY;
             }
         } else if (active) {
-            for (int r = r0; r < N; r += R, X += dX, Y += dY) xi[r * N + c] = sample_at(s, N, P, X, Y);
+            for (int r = r0; r < N; r += R, X += dX, Y += dY)
+                xi[r * N + c] = sample_at(s, N, Pa, X, Y);
         }
     }
     __syncthreads();
@@ -474,25 +480,25 @@ __global__ void __launch_bounds__(NT) rotate_kernel(
 #pragma unroll
         for (int k = 0; k < MAXV; ++k) {
             const int r = r0 + k * R;
-            if (active && r < N) s[r * P + c] = keep[k];
+            if (active && r < N) s[r * Pb + c] = keep[k];
         }
     } else {
         for (int p = threadIdx.x; p < NN; p += NT) {
             const int r = p / N, cc = p - r * N;
-            s[r * P + cc] = xi[p];
+            s[r * Pb + cc] = xi[p];
         }
     }
     __syncthreads();
-    prefilter_axis<NT>(s, N, P, 0, nseg, inv1mzN, exact_init != 0);
-    prefilter_axis<NT>(s, N, P, 1, nseg, inv1mzN, exact_init != 0);
-    fill_halo<NT>(s, N, P);
+    prefilter_axis<NT>(s, N, Pb, 0, nseg, inv1mzN, exact_init != 0);
+    prefilter_axis<NT>(s, N, Pb, 1, nseg, inv1mzN, exact_init != 0);
+    fill_halo<NT>(s, N, Pb);
     if (!active) return;
-    const RotConst Q = rot[1];
+    const RotConst& Q = q1;
     int64_t X = Q.bx + (int64_t)r0 * Q.rc + (int64_t)c * Q.rs;
     int64_t Y = Q.by - (int64_t)r0 * Q.rs + (int64_t)c * Q.rc;
     const int64_t dX = (int64_t)R * Q.rc, dY = -(int64_t)R * Q.rs;
     float* out = img_out + img * (int64_t)NN;
-    for (int r = r0; r < N; r += R, X += dX, Y += dY) out[r * N + c] = sample_at(s, N, P, X, Y);
+    for (int r = r0; r < N; r += R, X += dX, Y += dY) out[r * N + c] = sample_at(s, N, Pb, X, Y);
 }
 
 // Compile-time box size (power-of-two N, 512 threads): the same computation as rotate_kernel
@@ -1052,8 +1058,12 @@ int rotate(const mem_plan& P, const mem_inputs& in, float* xbuf, float* img_out,
         MEM_LAUNCH_CHECK();
         return MEM_OK;
     }
-    const int Pst = ((N + 3) % 2 == 0) ? N + 4 : N + 3;     // odd row stride, 3-px halo
-    const size_t smem = (size_t)(N + 3) * Pst * sizeof(float);
+    // row strides (3-px halo): 1 and -1 mod 32, picked per rotation by its angle, where the
+    // larger fits shared memory; else one odd stride for both
+    int P1 = ((N + 3 + 30) / 32) * 32 + 1, Pm1 = ((N + 3 + 32) / 32) * 32 - 1;
+    if ((size_t)(N + 3) * std::max(P1, Pm1) * sizeof(float) > 227 * 1024)
+        P1 = Pm1 = ((N + 3) % 2 == 0) ? N + 4 : N + 3;
+    const size_t smem = (size_t)(N + 3) * std::max(P1, Pm1) * sizeof(float);
     constexpr int NT = 512;
     if (N == 128 || N == 64) {
         auto kfn = N == 128 ? rotate_fixed_kernel<NT, 128> : rotate_fixed_kernel<NT, 64>;
@@ -1075,12 +1085,12 @@ int rotate(const mem_plan& P, const mem_inputs& in, float* xbuf, float* img_out,
         MEM_CUDA_TRY(cudaFuncSetAttribute(rotate_kernel<NT, 32>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         rotate_kernel<NT, 32><<<(unsigned)P.n_images, NT, smem, s>>>(
-            xbuf, img_out, rotc, N, Pst, nseg, inv1mzN, exact ? 1 : 0);
+            xbuf, img_out, rotc, N, P1, Pm1, nseg, inv1mzN, exact ? 1 : 0);
     } else {
         MEM_CUDA_TRY(cudaFuncSetAttribute(rotate_kernel<NT, 0>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         rotate_kernel<NT, 0><<<(unsigned)P.n_images, NT, smem, s>>>(
-            xbuf, img_out, rotc, N, Pst, nseg, inv1mzN, exact ? 1 : 0);
+            xbuf, img_out, rotc, N, P1, Pm1, nseg, inv1mzN, exact ? 1 : 0);
     }
     MEM_LAUNCH_CHECK();
     return MEM_OK;
