@@ -247,25 +247,6 @@ struct Fft2 {
             S[addr((R2 * k1 + t) >> 1, (t & 1) ? q1 : q0)] = k1 ? cmulc(v[t], W[t * k1]) : v[t];
     }
 
-    template <int K2>
-    static __device__ __forceinline__ void filter_packed(const float2* v, float2* y, int k1, int c,
-                                                         const float* __restrict__ gtab) {
-        if constexpr (K2 < R2) {
-            const float2 m = mirror<K2>(v, k1);
-            const int j = k1 + R1 * K2;
-            const int fa = min(j, N - j);
-            if (c == 0) {
-                const float g0 = __ldg(gtab + fa * HS), gh = __ldg(gtab + fa * HS + H);
-                const float gp = 0.5f * (g0 + gh), gm = 0.5f * (g0 - gh);
-                y[K2] = make_float2(v[K2].x * gp + m.x * gm, v[K2].y * gp - m.y * gm);
-            } else {
-                const float g = __ldg(gtab + fa * HS + c);
-                y[K2] = make_float2(v[K2].x * g, v[K2].y * g);
-            }
-            filter_packed<K2 + 1>(v, y, k1, c, gtab);
-        }
-    }
-
     // column pass 2 with the low-pass: forward DFT, multiply by G/N^2 (gtab [N][N/2+1];
     // G(j, .) = G(N-j, .)), inverse DFT
     static __device__ __forceinline__ void cols_filter(float2* S, const float2* W,
@@ -277,11 +258,43 @@ struct Fft2 {
             float2 v[R2];
             cols_forward2_load(S, c, k1, v);
             if (w == 0 && i == 0) {
-                // packed column: Y'[j] = Y[j] (G0 + Gh)/2 + conj Y[-j] (G0 - Gh)/2
-                float2 y[R2];
-                filter_packed<0>(v, y, k1, c, gtab);
+                // packed column (c = 0): Y'[j] = Y[j] (G0 + Gh)/2 + conj Y[-j] (G0 - Gh)/2.
+                // Its lanes leave their spectrum values in the column's own slots (read above,
+                // rewritten by cols_inverse1_store below; only this warp touches them) and read
+                // the mirrors Y[-j] back from there, so the filter is applied in place in v[]
+                // with no second register array.
+                const int q0 = pos(0), q1 = pos(H);
+                auto slot = [&](int kk1, int k2) {
+                    return addr((R2 * kk1 + k2) >> 1, (k2 & 1) ? q1 : q0);
+                };
+                if (c == 0) {
 #pragma unroll
-                for (int k2 = 0; k2 < R2; ++k2) v[k2] = y[k2];
+                    for (int k2 = 0; k2 < R2; ++k2) S[slot(k1, k2)] = v[k2];
+                }
+                __syncwarp();
+                if (c == 0) {
+                    // Y[-j] for j = k1 + R1 k2: lane (R1 - k1) mod R1's value at R2 - 1 - k2
+                    // (k1 > 0), this lane's at (R2 - k2) mod R2 (k1 = 0)
+                    const int mk1 = (R1 - k1) % R1;
+#pragma unroll
+                    for (int k2 = 0; k2 < R2; ++k2) {
+                        const float2 m =
+                            S[slot(mk1, k1 == 0 ? (R2 - k2) % R2 : R2 - 1 - k2)];
+                        const int j = k1 + R1 * k2;
+                        const int fa = min(j, N - j);
+                        const float g0 = __ldg(gtab + fa * HS), gh = __ldg(gtab + fa * HS + H);
+                        const float gp = 0.5f * (g0 + gh), gm = 0.5f * (g0 - gh);
+                        v[k2] = make_float2(v[k2].x * gp + m.x * gm, v[k2].y * gp - m.y * gm);
+                    }
+                } else {
+#pragma unroll
+                    for (int k2 = 0; k2 < R2; ++k2) {
+                        const int j = k1 + R1 * k2;
+                        const float g = __ldg(gtab + min(j, N - j) * HS + c);
+                        v[k2] = make_float2(v[k2].x * g, v[k2].y * g);
+                    }
+                }
+                __syncwarp();           // every mirror read before the slots are rewritten
             } else {
 #pragma unroll
                 for (int k2 = 0; k2 < R2; ++k2) {
@@ -499,7 +512,8 @@ __device__ __forceinline__ void lowpass_image(
     F::rows_inverse(S, W, dst);
 }
 
-// one image per CTA
+// one image per CTA (N = 128: two CTAs per SM; a register budget for three spills 52 bytes and
+// measured slower, 28.4 against 23.3 ms on config4)
 template <int N>
 __global__ void __launch_bounds__(2 * N, N == 128 ? 2 : 4) lowpass_fft_kernel(
         const float* __restrict__ stack, int64_t num_stack, const int64_t* __restrict__ sidx,
