@@ -45,6 +45,10 @@ struct TcShape {
     static constexpr int STAGE_BYTES = (2 + 2 * B_BOXES) * TC_OPB;
     static constexpr int STAGES = BN == 256 ? 2 : 3;
     static constexpr size_t SMEM = (size_t)STAGES * STAGE_BYTES + 1024 + 256;
+    // epilogue warps: 4 lane quadrants x BN / 64 column blocks of 64, so that every epilogue
+    // thread keeps 64 running sums (BN = 256 with 8 warps would keep 128 and spill)
+    static constexpr int EPI_WARPS = BN / 16;
+    static constexpr int THREADS = (EPI_WARPS + 2) * 32;
     static_assert(STAGES <= TC_MAX_STAGES, "stage ring");
 };
 
@@ -75,7 +79,7 @@ struct TcShared {
 // accumulators (NBUF x 128 columns) continue from one tile to the next, so a tile's first
 // groups are loaded and multiplied while the epilogue still adds and stores the previous tile.
 template <bool KAHAN, bool LOLO, int NBUF, int BN>
-__global__ void __launch_bounds__(TC_THREADS, 1) gemm_tc_kernel(
+__global__ void __launch_bounds__(TcShape<BN>::THREADS, 1) gemm_tc_kernel(
         const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CUtensorMap map_lo,
         const double* __restrict__ pair_norm, const uint32_t* __restrict__ scale_bits,
         const Tile* __restrict__ tiles, const PdDev* __restrict__ pds, double* __restrict__ D,
@@ -87,7 +91,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gemm_tc_kernel(
     using S = TcShape<BN>;
     constexpr int TC_STAGES = S::STAGES, TC_STAGE_BYTES = S::STAGE_BYTES;
     constexpr uint32_t IDESC = idesc_f16<BN>(), IDESC_NEG = IDESC | (1u << 14);
-    constexpr int EC = BN / 2;                     // epilogue columns per thread
+    constexpr int EPI = S::EPI_WARPS;              // epilogue warps (warps 0 .. EPI - 1)
+    constexpr int EC = 64;                         // epilogue columns per thread
     constexpr uint32_t TMEM_COLS = NBUF * BN;
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -108,13 +113,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gemm_tc_kernel(
         }
         for (int b = 0; b < NBUF; ++b) {
             mbar_init(&sh->acc_full[b], 1);
-            mbar_init(&sh->acc_empty[b], TC_EPI_WARPS);
+            mbar_init(&sh->acc_empty[b], EPI);
         }
         mbar_init(&sh->mma_done, 1);
         sh->abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == TC_EPI_WARPS + 1) {
+    if (warp == EPI + 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                          smem_u32(&sh->tmem_base)),
                      "r"(TMEM_COLS)
@@ -126,7 +131,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gemm_tc_kernel(
     tc_fence_after();
     const uint32_t tmem = sh->tmem_base;
 
-    if (warp == TC_EPI_WARPS) {
+    if (warp == EPI) {
         // ---------------------------------------------------------------- TMA producer
         if (lane == 0) {
             asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&map_hi) : "memory");
@@ -175,7 +180,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gemm_tc_kernel(
                                    wait_limit);
             }
         }
-    } else if (warp == TC_EPI_WARPS + 1) {
+    } else if (warp == EPI + 1) {
         // ---------------------------------------------------------------- MMA issuer
         if (lane == 0) {
             bool issued_any = false, stop = false;
@@ -263,17 +268,23 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gemm_tc_kernel(
                 tc_fence_after();
                 const uint32_t taddr =
                     tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN + h * EC);
+                // BN = 256 (16 epilogue warps, 112 registers each): 16-column loads, so that
+                // the 64 running sums and the loaded columns fit without spilling
+                constexpr int LDC = BN == 256 ? 16 : 32;
 #pragma unroll
-                for (int half = 0; half < EC / 32; ++half) {
-                    uint32_t r[32];
-                    tmem_ld32(taddr + half * 32, r);
+                for (int half = 0; half < EC / LDC; ++half) {
+                    uint32_t r[LDC];
+                    if constexpr (LDC == 16)
+                        tmem_ld16(taddr + half * LDC, r);
+                    else
+                        tmem_ld32(taddr + half * LDC, r);
                     tmem_ld_wait();
 #pragma unroll
-                    for (int j = 0; j < 32; ++j) {
+                    for (int j = 0; j < LDC; ++j) {
                         const float x = __uint_as_float(r[j]);
-                        float& s = acc[half * 32 + j];
+                        float& s = acc[half * LDC + j];
                         if (KAHAN) {
-                            float& c = cmp[KAHAN ? half * 32 + j : 0];
+                            float& c = cmp[KAHAN ? half * LDC + j : 0];
                             const float y = x - c;
                             const float tt = s + y;
                             c = (tt - s) - y;
@@ -301,6 +312,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gemm_tc_kernel(
 #pragma unroll
                 for (int j = 0; j < EC; ++j) {
                     const int gj = j0 + j;
+                    // blocks of 8 columns: keeps the compiler from hoisting all 64 norm loads
+                    // ahead of the stores (their registers would spill the running sums)
+                    if ((j & 7) == 0) asm volatile("" ::: "memory");
                     if (gj >= n || gj < gi) continue;
                     if (gj == gi) {
                         Dp[(int64_t)gi * n + gi] = 0.0;
@@ -316,7 +330,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gemm_tc_kernel(
     }
     tc_fence_before();
     __syncthreads();
-    if (warp == TC_EPI_WARPS + 1) {
+    if (warp == EPI + 1) {
         tc_fence_after();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                      "r"(TMEM_COLS)
@@ -647,7 +661,8 @@ int gemm_split_bf16(const mem_plan& P, const void* feat_hi, const void* feat_lo,
         MEM_CUDA_TRY(cudaFuncSetAttribute(gemm_tc_kernel<KAHAN, LOLO, NB, BN>,                 \
                                           cudaFuncAttributeMaxDynamicSharedMemorySize,         \
                                           (int)TcShape<BN>::SMEM));                            \
-        gemm_tc_kernel<KAHAN, LOLO, NB, BN><<<grid, TC_THREADS, TcShape<BN>::SMEM, s>>>(       \
+        gemm_tc_kernel<KAHAN, LOLO, NB, BN><<<grid, TcShape<BN>::THREADS, TcShape<BN>::SMEM,   \
+                                              s>>>(                                            \
             mhi, mlo, pair_norm, scale_bits, tiles, pds, D, status, chunks, P.n_chunks,        \
             P.tc_group_chunks, P.wait_cycles, P.test_withhold_chunk, begin, count);            \
     } while (0)
