@@ -564,7 +564,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(TC_THREADS, 1) gemm_
                 }
                 tc_fence_before();
                 __syncwarp();
-                if (lane == 0) mbar_arrive_cluster(acc_empty_even + 8u * (uint32_t)b);
+                // the accumulator's columns are in registers (tcgen05.wait::ld above): a relaxed
+                // arrive suffices, and a release at cluster scope cost a memory barrier per
+                // warp and group (the kernel's top stall)
+                if (lane == 0) mbar_arrive_cluster_relaxed(acc_empty_even + 8u * (uint32_t)b);
             }
             if (!ok || *abort_flag) break;
             const PdDev pd = pds[t.pd];

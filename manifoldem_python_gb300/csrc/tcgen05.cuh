@@ -162,8 +162,11 @@ __device__ __forceinline__ void cluster_sync() {
 }
 
 // arrive on a barrier of another CTA of the cluster (cluster address from map_to_cta)
-__device__ __forceinline__ void mbar_arrive_cluster(uint32_t cluster_addr) {
-    asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(cluster_addr)
+// An arrive on a barrier of either CTA of the pair (cluster address) without release
+// semantics: for an arrive that only has to follow reads this thread has already waited for
+// (tcgen05.wait::ld), so that no memory barrier is issued
+__device__ __forceinline__ void mbar_arrive_cluster_relaxed(uint32_t cluster_addr) {
+    asm volatile("mbarrier.arrive.relaxed.cluster.shared::cluster.b64 _, [%0];" ::"r"(cluster_addr)
                  : "memory");
 }
 
