@@ -774,8 +774,8 @@ __global__ void __launch_bounds__(256) pd_finalize_kernel(
 //     V_j(R) = C_j(m_R)^2 - mt(R): one column per ring, rings by decreasing |k|^2.  Phase 1
 //     keeps sw u' of every frequency in shared memory at its position in ring order, phase 2
 //     sums each ring's contiguous range.
-template <int MODE, bool RINGS>
-__global__ void __launch_bounds__(256) features_kernel(
+template <int MODE, bool RINGS, int NT>
+__global__ void __launch_bounds__(NT) features_kernel(
         float2* __restrict__ spec, const uint64_t* __restrict__ qfix,
         const PdDev* __restrict__ pds, const int32_t* __restrict__ img_pd,
         const int32_t* __restrict__ img_row, const FeatTables ft,
@@ -897,7 +897,7 @@ __global__ void __launch_bounds__(256) features_kernel(
     };
     // two consecutive slots per thread: they share a 64-wide chunk, so their feature columns
     // are adjacent (col even) and each block gets one paired store
-    for (int64_t k = 2 * (int64_t)threadIdx.x; k < Kc_pad; k += 512) {
+    for (int64_t k = 2 * (int64_t)threadIdx.x; k < Kc_pad; k += 2 * NT) {
         float f0[4], f1[4];
         if (pair_loads && k < Kc) {
             feature_pair(k, f0, f1);
@@ -927,7 +927,7 @@ __global__ void __launch_bounds__(256) features_kernel(
             *U = su;
             *V = (C * C - mu[4 * Kc_pad + R]) * sc;
         };
-        for (int64_t R = 2 * (int64_t)threadIdx.x; R < Kr_pad; R += 512) {
+        for (int64_t R = 2 * (int64_t)threadIdx.x; R < Kr_pad; R += 2 * NT) {
             float U0, V0, U1, V1;
             ring(R, &U0, &V0);
             ring(R + 1, &U1, &V1);
@@ -936,12 +936,12 @@ __global__ void __launch_bounds__(256) features_kernel(
         }
     }
     const float2 a2 = acc2.value();
-    const double a = block_sum_double<256>((double)acc.value() + (double)a2.x + (double)a2.y,
-                                           red);
+    const double a = block_sum_double<NT>((double)acc.value() + (double)a2.x + (double)a2.y,
+                                          red);
     if (threadIdx.x == 0) pair_norm[img] = a;
     if (ctf_out) {
         float* co = ctf_out + img * (int64_t)N * N;
-        for (int p = threadIdx.x; p < N * N; p += 256) {
+        for (int p = threadIdx.x; p < N * N; p += NT) {
             const int r = p / N, c = p - r * N;
             const int fa = min(r, N - r), fb = min(c, N - c);
             int sg;
@@ -1138,15 +1138,23 @@ int features(const mem_plan& P, float2* spec, const uint64_t* qf, const PdDev* p
              cudaStream_t s) {
     if (P.n_images == 0) return MEM_OK;
     const size_t smem = P.ring_features ? sizeof(float) * P.Kc : 0;
-#define MEM_FEATS(MODE, RINGS)                                                                 \
+    // 256 threads per image; 1024 when the ring table leaves room for fewer than three CTAs
+    // per SM (large boxes: 126 KB at 250 px), so that the SM still holds 32 warps
+    const bool wide = smem > 72 * 1024;
+#define MEM_FEATS_NT(MODE, RINGS, NT)                                                          \
     do {                                                                                       \
-        MEM_CUDA_TRY(cudaFuncSetAttribute(features_kernel<MODE, RINGS>,                        \
+        MEM_CUDA_TRY(cudaFuncSetAttribute(features_kernel<MODE, RINGS, NT>,                    \
                                           cudaFuncAttributeMaxDynamicSharedMemorySize,         \
                                           (int)smem));                                         \
-        features_kernel<MODE, RINGS><<<(unsigned)P.n_images, 256, smem, s>>>(                  \
+        features_kernel<MODE, RINGS, NT><<<(unsigned)P.n_images, NT, smem, s>>>(               \
             spec, qf, pds, img_pd, img_row, ft, means, scale_bits, feat_a, feat_b, pair_norm,  \
             ctf_out, (float2*)spectrum_out, P.N, P.Nh, P.Kc, P.Kc_pad, P.Kr, P.Kr_pad,         \
             means_stride(P), P.ctf, write_signed ? 1 : 0, P.Kc % 2 == 0 ? 1 : 0);              \
+    } while (0)
+#define MEM_FEATS(MODE, RINGS)                                                                 \
+    do {                                                                                       \
+        if (wide) MEM_FEATS_NT(MODE, RINGS, 1024);                                             \
+        else MEM_FEATS_NT(MODE, RINGS, 256);                                                   \
     } while (0)
     const bool bf16 = P.params.precision == MEM_PREC_SPLIT_BF16;
     if (P.ring_features) {
@@ -1157,6 +1165,7 @@ int features(const mem_plan& P, float2* spec, const uint64_t* qf, const PdDev* p
         else MEM_FEATS(0, false);
     }
 #undef MEM_FEATS
+#undef MEM_FEATS_NT
     MEM_LAUNCH_CHECK();
     return MEM_OK;
 }
