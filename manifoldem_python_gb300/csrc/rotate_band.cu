@@ -1,7 +1,8 @@
 // The two periodic cubic B-spline rotations of rotatefill.op (modules/rotatefill.py:21-41,
 // called at modules/getDistanceCTF_local_Conj9combinedS2.py:328-330) for boxes whose
 // coefficient image does not fit one CTA's shared memory (64 < N <= 512 without a compile-time
-// kernel; N = 250 is the 1500-PD workload's box).  One CTA of 512 threads per image.
+// kernel; N = 250 is the 1500-PD workload's box).  One CTA per image (512 threads, one CTA per
+// SM, by default; the launcher's variants are described at rotate_band).
 //
 // Each rotation is split where the separable prefilter splits:
 //   1. the prefilter along layout columns (every line runs across all N layout rows), from the
