@@ -417,11 +417,36 @@ def kernels_per_execute(outputs, avg_only, N, counts=None, classes=None):
 
 def traffic_from_profiles(kernel_tag, workload):
     """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary, if any."""
+    return profile_number(kernel_tag, workload, 'traffic_bytes_per_full_launch')
+
+
+def profile_number(kernel_tag, workload, key):
+    """A `key: value` figure from the committed ncu summary of the kernel, if any."""
     path = os.path.join(HERE, 'profiles', '%s_%s.md' % (kernel_tag, workload))
     if not os.path.exists(path):
         return None
-    m = re.search(r'traffic_bytes_per_full_launch:\s*([0-9.eE+]+)', open(path).read())
+    m = re.search(key + r':\s*([0-9.eE+]+)', open(path).read())
     return float(m.group(1)) if m else None
+
+
+def shared_memory_roofline(r, args, phase):
+    """The shared-memory bound of a phase whose kernel is limited by shared-memory wavefronts
+    (the rotation): wavefronts per image from the committed ncu summary of the kernel x the
+    images / the phase's live time, against one wavefront per SM per clock at the SM clock
+    sampled during the timed region."""
+    per_img = profile_number(phase, args.config, 'shared_wavefronts_per_image')
+    mhz = (r.get('clocks') or {}).get('sm_mhz')
+    if not per_img or not mhz:
+        return None
+    import torch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    ach = per_img * r['n_images'] / (r['phases'][phase] * 1e-3)
+    peak = sms * mhz * 1e6
+    return dict(achieved=ach, peak=peak, unit='wavefronts/s', frac=ach / peak,
+                wavefronts_per_image=per_img,
+                source='profiles/%s_%s.md (ncu l1tex__data_pipe_lsu_wavefronts_mem_shared.sum '
+                       'per image); peak = %d SMs x 1 wavefront per clock x %.0f MHz'
+                       % (phase, args.config, sms, mhz))
 
 
 def time_form(plan, stack, sidx, flip, psi, dfd, outs, args, world, dev, flush):
@@ -1122,6 +1147,9 @@ def main():
         clocks=r['clocks'],
         gpu_launches=r['kernels'] * args.steps,
     )
+    smem_rl = shared_memory_roofline(r, args, rl['phase']) if rl['bound'] == 'hbm' else None
+    if smem_rl:
+        line['roofline']['shared_memory'] = smem_rl
     if r['e2e']:
         e = r['e2e']
         line['e2e'] = dict(value=pairs_total / (e['ms'] * 1e-3), unit='pairs/s',
