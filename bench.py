@@ -421,12 +421,13 @@ def traffic_from_profiles(kernel_tag, workload):
 
 
 def profile_number(kernel_tag, workload, key):
-    """A `key: value` figure from the committed ncu summary of the kernel, if any."""
+    """A `key: value` figure from the committed ncu summary of the kernel, if any (the last
+    one: summaries append the capture of each newer build at the end)."""
     path = os.path.join(HERE, 'profiles', '%s_%s.md' % (kernel_tag, workload))
     if not os.path.exists(path):
         return None
-    m = re.search(key + r':\s*([0-9.eE+]+)', open(path).read())
-    return float(m.group(1)) if m else None
+    found = re.findall(key + r':\s*([0-9.eE+]+)', open(path).read())
+    return float(found[-1]) if found else None
 
 
 def shared_memory_roofline(r, args, phase):

@@ -197,7 +197,7 @@ def test_fused_image_stage_matches_three_kernels(cuda_ready, N):
         assert e < 1e-6, (k, e)
 
 
-@pytest.mark.parametrize('N', [96, 250, 300, 512])
+@pytest.mark.parametrize('N', [96, 230, 250, 300, 512])
 def test_band_rotation_matches_whole_image_kernels(cuda_ready, N):
     """The banded rotation (coefficient image in bands of rows in shared memory, the column
     prefilter through global memory) against the whole-image kernels on the same inputs

@@ -158,3 +158,20 @@ def test_stack_runs_split_and_remap():
     np.testing.assert_array_equal(remap, np.arange(100)[::-1])
     runs, remap = stack_runs(np.array([], dtype=np.int64), 1)
     assert runs == [] and remap.size == 0
+
+
+def test_bench_reads_profile_figures():
+    """The figures bench.py takes from the committed ncu summaries: the rotation's DRAM traffic
+    per full config4 launch and its shared-memory wavefronts per image (config4 and config5),
+    and the contraction's traffic."""
+    import importlib.util
+    import os
+    here = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    spec = importlib.util.spec_from_file_location('bench_module', os.path.join(here, 'bench.py'))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    assert bench.traffic_from_profiles('rotate', 'config4') == 4.82e10
+    assert bench.profile_number('rotate', 'config4', 'shared_wavefronts_per_image') == 36790
+    assert bench.profile_number('rotate', 'config5', 'shared_wavefronts_per_image') == 149825
+    assert bench.traffic_from_profiles('contraction_bf16x3', 'config4') == 3.11e10
+    assert bench.profile_number('rotate', 'config3', 'shared_wavefronts_per_image') is None
