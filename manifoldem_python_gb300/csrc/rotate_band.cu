@@ -227,7 +227,7 @@ __device__ __forceinline__ void rotate_banded(const float* in, float* A, float* 
         }
         __syncthreads();
         // 2b. along layout rows, in shared memory (lanes on consecutive rows: the row stride is
-        // 1 mod 32, so a warp's 32 accesses fall in 32 banks)
+        // +-1 mod 32, so a warp's 32 accesses fall in 32 banks)
         prefilter_lines<NT, false, false>(rows, N, nsg, zlast, carry, s, s, P, 1);
         for (int p = threadIdx.x; p < rows * 3; p += NT) {
             const int rho = p / 3, j = p - rho * 3;
