@@ -148,11 +148,12 @@ def test_dropin_op_writes_reference_pickle(cuda_ready):
     assert d['options'] == options
 
 
-@pytest.mark.parametrize('N', [64, 128, 192, 250, 512])
+@pytest.mark.parametrize('N', [64, 96, 128, 192, 250, 300, 512])
 def test_box_sizes_match_oracle(cuda_ready, N):
     """Box sizes with their own kernels, against the FP64 oracle on a small PD with conjugate
-    views: 64 and 128 px (shared-memory FFTs, compile-time-size rotation), the 192 px workload
-    size (cuFFT), 250 px (rotation with global-memory coefficients) and 512 px, the largest box
+    views: 64 and 128 px (shared-memory FFTs, compile-time-size rotation), 96 and the 192 px
+    workload size (cuFFT, whole-image rotation with a per-angle row stride), 250 and 300 px
+    (banded rotation; 300 px with a short last prefilter segment) and 512 px, the largest box
     (per-frequency U', V' features: its half plane exceeds the ring-feature buffer)."""
     torch = cuda_ready
     import dataclasses
